@@ -1,0 +1,59 @@
+"""ctypes binding of libbpl_gb300.so (the C ABI declared in include/bpl_gb300.h).
+
+The library is built in-tree by bpl_gb300._build.build() (called by
+__graft_entry__.build()).  There is no fallback: if the library is missing
+every op raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from ._build import LIB_PATH
+
+_lib = None
+
+c_int, c_float, c_void_p = ctypes.c_int, ctypes.c_float, ctypes.c_void_p
+
+# name -> argtypes (all functions return int status unless listed in _RESTYPE)
+SIGNATURES = {
+    "bpl_version": [],
+    "bpl_status_string": [c_int],
+    "bpl_last_error": [],
+    "bpl_read_device_error": [c_void_p],
+    "bpl_lbp_forward": [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p] + [c_int] * 8 + [c_void_p],
+}
+_RESTYPE = {"bpl_status_string": ctypes.c_char_p, "bpl_last_error": ctypes.c_char_p}
+
+
+class BplError(RuntimeError):
+    pass
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise BplError(
+                "libbpl_gb300.so is not built (expected at %s); run bpl_gb300._build.build() "
+                "or __graft_entry__.build() first" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPE.get(name, c_int)
+        _lib = L
+    return _lib
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        L = lib()
+        raise BplError("%s failed: %s: %s" % (what, L.bpl_status_string(status).decode(),
+                                                L.bpl_last_error().decode()))
+
+
+def read_device_error() -> int:
+    code = ctypes.c_int(0)
+    check(lib().bpl_read_device_error(ctypes.byref(code)), "bpl_read_device_error")
+    return code.value

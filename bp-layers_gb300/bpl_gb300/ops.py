@@ -1,0 +1,85 @@
+"""torch-tensor front end of the C ABI.
+
+Each function checks its inputs the way the reference's pybind glue does
+(CUDA, contiguous: ops/lbp_stereo/src/lbp.cpp:8-10) plus dtype and shape,
+allocates outputs with torch on the input's device, and enqueues the CUDA
+kernels on torch's current stream.  Errors raise BplError (the reference
+aborts the process on CUDA errors; ops/include/error_util.h:13-23).
+"""
+from __future__ import annotations
+
+import torch
+
+from ._lib import BplError, check, lib
+
+LBP_STEREO, LBP_SEM_GLOBAL, LBP_SEM_PIXEL = 0, 1, 2
+ARGMIN_NONE, ARGMIN_F32, ARGMIN_U8, ARGMIN_U16 = 0, 1, 2, 3
+
+_ARGMIN_KIND = {torch.float32: ARGMIN_F32, torch.uint8: ARGMIN_U8, torch.int16: ARGMIN_U16,
+                torch.uint16 if hasattr(torch, "uint16") else torch.int16: ARGMIN_U16}
+
+
+def _stream(t: torch.Tensor) -> int:
+    return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def _check_input(name: str, t: torch.Tensor, dtype=torch.float32, dim=None):
+    if not isinstance(t, torch.Tensor):
+        raise BplError(f"{name} must be a tensor")
+    if not t.is_cuda:
+        raise BplError(f"{name} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise BplError(f"{name} must be contiguous")
+    if dtype is not None and t.dtype != dtype:
+        raise BplError(f"{name} must be {dtype}, got {t.dtype}")
+    if dim is not None and t.dim() != dim:
+        raise BplError(f"{name} must have {dim} dimensions, got {t.dim()}")
+
+
+def _ptr(t):
+    return t.data_ptr() if t is not None else None
+
+
+def lbp_forward(variant: int, cost: torch.Tensor, jump: torch.Tensor, edge: torch.Tensor,
+                messages: torch.Tensor, delta: int, argmin_dtype=torch.float32, argmin=None,
+                scale=None):
+    """One LBP pass (RIGHT, LEFT, DOWN, UP sweeps), messages updated in place.
+
+    Returns (messages, argmin, scale).  argmin has the messages' shape and
+    `argmin_dtype` (float32 like the reference, or uint8/int16 for the
+    compact storage); None skips storing it.  Preallocated argmin/scale
+    buffers may be passed to avoid allocation.
+    """
+    _check_input("cost", cost, dim=4)
+    _check_input("edge", edge, dim=4)
+    _check_input("messages", messages, dim=5)
+    _check_input("jump", jump)
+    B, H, W, L = cost.shape
+    if tuple(messages.shape) != (B, 4, H, W, L):
+        raise BplError(f"messages must be {(B, 4, H, W, L)}, got {tuple(messages.shape)}")
+    if edge.shape[1:] != (4, H, W) or edge.shape[0] not in (1, B):
+        raise BplError(f"edge must be (B|1,4,H,W), got {tuple(edge.shape)}")
+    Lv, jb = 0, 1
+    if variant == LBP_STEREO:
+        if jump.dim() != 5 or jump.shape[1] != 4 or jump.shape[3:] != (H, W) or jump.shape[0] not in (1, B):
+            raise BplError(f"stereo jump must be (B|1,4,Lv,H,W), got {tuple(jump.shape)}")
+        Lv, jb = jump.shape[2], jump.shape[0]
+    elif variant == LBP_SEM_GLOBAL:
+        if tuple(jump.shape[1:]) != (4, L, L):
+            raise BplError(f"semantic jump must be (1,4,L,L), got {tuple(jump.shape)}")
+    else:
+        if tuple(jump.shape) != (4, H, W, L, L):
+            raise BplError(f"pixel jump must be (4,H,W,L,L), got {tuple(jump.shape)}")
+    if argmin_dtype is None:
+        kind = ARGMIN_NONE
+        argmin = None
+    else:
+        kind = _ARGMIN_KIND[argmin_dtype]
+        if argmin is None:
+            argmin = torch.zeros((B, 4, H, W, L), dtype=argmin_dtype, device=cost.device)
+    if scale is None:
+        scale = torch.zeros((B, 4, H, W), dtype=torch.float32, device=cost.device)
+    st = lib().bpl_lbp_forward(variant, _ptr(cost), _ptr(jump), _ptr(edge), _ptr(messages), _ptr(argmin), kind,
+                               _ptr(scale), B, H, W, L, Lv, jb, edge.shape[0], int(delta), _stream(cost))
+    check(st, "bpl_lbp_forward")
+    return messages, argmin, scale

@@ -1,0 +1,92 @@
+/*
+ * bpl_gb300.h -- C ABI of the GB300-native BP-Layers hot path.
+ *
+ * Every entry point takes caller-owned device pointers, plain sizes and a
+ * CUDA stream (passed as void*; NULL = legacy default stream), enqueues its
+ * kernels on that stream and returns a status code.  Nothing here
+ * synchronises the device, exits the process or allocates device memory
+ * unless stated.  All tensors are dense, contiguous, row-major float32 unless
+ * stated, with the reference's layouts:
+ *
+ *   cost      (B,H,W,L)        messages / argmin  (B,4,H,W,L)
+ *   edge      (Be,4,H,W)       scale              (B,4,H,W)
+ *   stereo jump taps  (Bj,4,Lv,H,W)  [offset, ..., 0 at Lv/2, ...]
+ *   semantic global   (1,4,L,L)      jump[d][s][t] = cost of label t given s
+ *   semantic pixel    (4,H,W,L,L)
+ *   direction index:  LEFT=0, RIGHT=1, UP=2, DOWN=3; message slot k at a
+ *   pixel holds the message received from the neighbour on side k.
+ *
+ * Differences from the reference ops (deliberate, documented):
+ *   - every batch item is processed (the reference forward/SAD/flow kernels
+ *     only process batch item 0);
+ *   - argmin may be stored as float32 (reference layout), uint8 or uint16.
+ */
+#ifndef BPL_GB300_H
+#define BPL_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define BPL_OK 0
+#define BPL_ERR_INVALID_ARG 1
+#define BPL_ERR_UNSUPPORTED 2
+#define BPL_ERR_CUDA 3
+#define BPL_ERR_DEVICE_TIMEOUT 4
+
+/* LBP pairwise variants */
+#define BPL_LBP_STEREO 0      /* ops/lbp_stereo            */
+#define BPL_LBP_SEM_GLOBAL 1  /* ops/lbp_semantic_pw       */
+#define BPL_LBP_SEM_PIXEL 2   /* ops/lbp_semantic_pw_pixel */
+
+/* argmin storage */
+#define BPL_ARGMIN_NONE 0
+#define BPL_ARGMIN_F32 1
+#define BPL_ARGMIN_U8 2
+#define BPL_ARGMIN_U16 3
+
+/* library version (major*10000 + minor*100 + patch) */
+int bpl_version(void);
+
+/* static text for a status code */
+const char* bpl_status_string(int status);
+
+/* message describing the last failure of a call made on this host thread */
+const char* bpl_last_error(void);
+
+/* Reads and clears the device error word that kernels set when one of their
+ * bounded waits runs out (synchronises the current device).  *code receives 0
+ * when no kernel reported an error. */
+int bpl_read_device_error(int* code);
+
+/*
+ * Min-sum LBP forward: one pass of the four directional sweeps (RIGHT, LEFT,
+ * DOWN, UP), messages updated in place.
+ * Replaces cuda::lbp_forward_min_sum / lbp_reduction_min_sum
+ *   ops/lbp_stereo/src/lbp_min_sum_kernel.cu:424-508   (variant STEREO)
+ *   ops/lbp_semantic_pw/src/lbp_min_sum_kernel.cu:424-510   (SEM_GLOBAL)
+ *   ops/lbp_semantic_pw_pixel/src/lbp_min_sum_kernel.cu:421-506 (SEM_PIXEL)
+ * bound in Python as `forward_minsum` (ops/lbp_stereo/src/lbp.cpp:16-27, :53).
+ *
+ * jump_batch / edge_batch: leading extent of jump (stereo only) and edge,
+ * 1 (broadcast) or B.  Lv: number of stereo jump taps (2..16; ignored for the
+ * semantic variants).  delta: truncation half-width (the reference's uint16
+ * `delta`; delta >= L selects the full O(L^2) minimisation).  argmin: output
+ * of `argmin_kind` type laid out like messages, or NULL with
+ * BPL_ARGMIN_NONE.  scale: (B,4,H,W) per-message exp-sum.  Only the
+ * receiving positions of each sweep are written (as in the reference); the
+ * caller zero-fills argmin/scale if it needs the rest defined.
+ * L: 1..1024.  Results are bit-identical to the reference's arithmetic.
+ */
+int bpl_lbp_forward(int variant, const float* cost, const float* jump, const float* edge,
+                    float* messages, void* argmin, int argmin_kind, float* scale, int B, int H,
+                    int W, int L, int Lv, int jump_batch, int edge_batch, int delta, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BPL_GB300_H */
