@@ -1,0 +1,383 @@
+"""Benchmark of the BP-Layers hot path on GB300.
+
+Workload (the full-size stereo configuration): one training step of the
+stereo BP layer, FP32, B=1, H=376, W=1240, D=L=192 labels, 3 message-passing
+iterations, truncated-linear pairwise with learnable L1=0.1 / L2=0.5
+(delta=3), per-pixel/direction edge weights exp(N(0,0.3)), forward
+(MessagePassing: 3 LBP passes, beliefs, softmin) and backward with an
+upstream gradient N(0,1) on the beliefs.  The cost volume comes from a
+synthetic piecewise-planar stereo scene (C=64 features, SAD over 192
+disparities, softmax) built once on the device before timing.
+
+One step = U = 2 * iters * L * (2H(W-1) + 2W(H-1)) message-label updates
+(forward + backward).  `value` = U * steps / device time with all inputs
+resident in HBM; `e2e` = the same step through the public API with the cost
+volume, edge weights and upstream gradient copied from pinned host memory and
+the cost gradient plus the disparity map copied back, every step.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+With --gpus N > 1 (launched by torchrun) every rank runs an independent
+replica on its own GPU (the path does not shard; no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "bp-layers_gb300"), os.path.join(ROOT, "tests", "golden")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "min-sum msg-label updates/s & HBM GB/s vs peak; served p50/p99 vs plain"
+UNIT = "msg-label updates/s"
+H, W, L, C_FEAT, ITERS, DELTA = 376, 1240, 192, 64, 3, 3
+FWD_BYTES_PER_UPDATE = 21  # cost + 3 incoming + 1 outgoing message (FP32) + 1 B argmin
+BWD_BYTES_PER_UPDATE = 17  # argmin + upstream grad + saved message + RMW grad-cost
+CPU_CROP_W = 310           # CPU baseline sample: one pass on a 376 x 310 x 192 crop
+
+
+def edges(h, w):
+    return 2 * h * (w - 1) + 2 * w * (h - 1)
+
+
+def updates_per_step(h=H, w=W, l=L, iters=ITERS):
+    return 2 * iters * l * edges(h, w)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sms.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
+                "samples": len(sms), "reasons": sorted(reasons)}
+
+
+def synth_inputs(torch, dev, seed):
+    """Piecewise-planar stereo scene -> SAD (C=64, D=192) -> softmax -> prob volume."""
+    import numpy as np
+    import cases
+    g = cases.rng(seed)
+    f0 = torch.from_numpy(g.normal(0.0, 1.0, size=(1, C_FEAT, H, W)).astype(np.float32)).to(dev)
+    disp = torch.from_numpy(cases.planar_disparity(g, H, W, L)).to(dev)
+    xs = torch.arange(W, device=dev).view(1, W).expand(H, W)
+    src = (xs + disp.round().long()).clamp(0, W - 1)
+    f1 = torch.gather(f0, 3, src.view(1, 1, H, W).expand(1, C_FEAT, H, W))
+    f1 = f1 + 0.1 * torch.randn(f1.shape, device=dev, generator=torch.Generator(device=dev).manual_seed(seed))
+    sad = torch.full((1, H, W, L), 40.0, device=dev)
+    for d in range(L):
+        if d < W:
+            sad[0, :, d:, d] = (f0[0, :, :, d:] - f1[0, :, :, :W - d]).abs().sum(0)
+    prob = torch.softmax(-sad, dim=-1).contiguous()
+    gen = torch.Generator(device=dev).manual_seed(seed + 1)
+    edge = torch.exp(0.3 * torch.randn((1, 4, H, W), device=dev, generator=gen)).contiguous()
+    upstream = torch.randn((1, H, W, L), device=dev, generator=gen).contiguous()
+    return prob, edge, upstream
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from bpl_gb300 import ops
+    from bpl_gb300.layers.stereo import MessagePassing
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    prob, edge, upstream = synth_inputs(torch, dev, seed=1 + rank)
+    mp = MessagePassing(dev, ITERS, L, DELTA)
+    with torch.no_grad():
+        mp._L1.fill_(0.1)
+        mp._L2.fill_(0.5)
+    prob.requires_grad_(True)
+
+    def step(p, e, g):
+        messages = torch.zeros((1, 4, H, W, L), device=dev, requires_grad=True)
+        beliefs, _ = mp(p, e, None, None, messages)
+        beliefs.backward(g)
+        return beliefs
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        prob.grad = None
+        step(prob, edge, upstream)
+    barrier()
+
+    stream = torch.cuda.current_stream()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk, ops.timing() as tm:
+        barrier()
+        torch.cuda.profiler.start()  # profiler range = the timed region (ncu --profile-from-start off)
+        t0.record(stream)
+        for _ in range(args.steps):
+            prob.grad = None
+            step(prob, edge, upstream)
+        t1.record(stream)
+        barrier()
+        torch.cuda.profiler.stop()
+    ms = t0.elapsed_time(t1)
+    per_op = tm.report()
+    ms_max = ms
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+
+    # ---- e2e through the public API with host buffers --------------------
+    prob_h = prob.detach().cpu().pin_memory()
+    edge_h = edge.cpu().pin_memory()
+    up_h = upstream.cpu().pin_memory()
+    grad_h = torch.empty(prob_h.shape, dtype=torch.float32).pin_memory()
+    disp_h = torch.empty((1, H, W, 1), dtype=torch.int64).pin_memory()
+    h2d = (prob_h.numel() + edge_h.numel() + up_h.numel()) * 4
+    d2h = grad_h.numel() * 4 + disp_h.numel() * 8
+
+    def e2e_step():
+        p = prob_h.to(dev, non_blocking=True).requires_grad_(True)
+        e = edge_h.to(dev, non_blocking=True)
+        g = up_h.to(dev, non_blocking=True)
+        beliefs = step(p, e, g)
+        grad_h.copy_(p.grad, non_blocking=True)
+        disp_h.copy_(torch.argmax(beliefs.detach(), dim=3, keepdim=True), non_blocking=True)
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    U = updates_per_step()
+    value = U * args.steps * world / (ms_max / 1e3)
+    e2e_value = U * args.steps * world / (e2e_ms / 1e3)
+    peak, peak_kind = load_peaks()
+    fwd = per_op.get("lbp_forward", [])
+    bwd = per_op.get("lbp_backward", [])
+    U_pass = L * edges(H, W)
+    fwd_ms = sum(fwd) / max(len(fwd), 1)
+    bwd_ms = sum(bwd) / max(len(bwd), 1)
+    if sum(fwd) >= sum(bwd):
+        kname, kms, kbytes = "lbp_forward_kernel", fwd_ms, U_pass * FWD_BYTES_PER_UPDATE
+    else:
+        kname, kms, kbytes = "lbp_backward_kernel", bwd_ms, U_pass * BWD_BYTES_PER_UPDATE
+    achieved = kbytes / (kms / 1e3) / 1e9
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "stereo BP-Layer forward+backward, 376x1240x192, 3 iterations, FP32",
+                   "B": 1, "H": H, "W": W, "L": L, "iters": ITERS, "delta": DELTA,
+                   "updates_per_step": U, "l2": "inputs larger than L2 (cost 358 MB, messages 1.43 GB)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms / args.steps},
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "launch_ms": kms, "algorithmic_bytes_per_launch": kbytes,
+                     "launch": "one pass = 2 grid launches (horizontal, vertical sweeps)"},
+        "kernel_ms": {"lbp_forward_pass": fwd_ms, "lbp_backward_pass": bwd_ms,
+                      "forward_GBps_21B": U_pass * FWD_BYTES_PER_UPDATE / (fwd_ms / 1e3) / 1e9 if fwd else None,
+                      "backward_GBps_17B": U_pass * BWD_BYTES_PER_UPDATE / (bwd_ms / 1e3) / 1e9 if bwd else None},
+        "gpu_launches": args.steps * ITERS * 2 * 2,
+        "clocks": clk.summary(),
+    }
+    traffic = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic):
+        with open(traffic) as fh:
+            tr = json.load(fh).get(kname)
+        if tr:
+            result["roofline"]["traffic"] = tr
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline_sample()
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(result))
+
+
+def cpu_sample_inputs(wc=CPU_CROP_W):
+    import numpy as np
+    import cases
+    g = cases.rng(5)
+    cost = cases.random_cost(g, 1, H, wc, L)
+    jump = cases.stereo_taps(1, H, wc, 0.1, 0.5)
+    edge = cases.edge_weights(g, 1, H, wc)
+    msgs = np.zeros((1, 4, H, wc, L), np.float32)
+    gin = g.normal(0, 1, size=(1, 4, H, wc, L)).astype(np.float32)
+    return cost, jump, edge, msgs, gin
+
+
+def cpu_pass(inputs, threads):
+    """One forward pass + reference adjoint with the oracle (the reference
+    has no CPU implementation of this path)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    cost, jump, edge, msgs, gin = inputs
+    m, am, sc = oracle.lbp_forward(0, cost, jump, edge, msgs, DELTA, threads=threads)
+    oracle.lbp_backward_ref(0, jump, edge, gin, m, am, sc, threads=threads)
+
+
+def cpu_baseline_sample():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    threads = os.cpu_count() or 1
+    inp = cpu_sample_inputs()
+    t = time.perf_counter()
+    cpu_pass(inp, threads)
+    dt = time.perf_counter() - t
+    U = 2 * L * edges(H, CPU_CROP_W)
+    return {"value": U / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle (C++/OpenMP, FP32 emulation forward + double reference adjoint), one pass "
+                      f"forward+backward on a {H}x{CPU_CROP_W}x{L} crop of the workload, {dt:.2f} s",
+            "max_threads": oracle.max_threads()}
+
+
+def run_reference(args):
+    """The reference has no CPU implementation of the path; its arithmetic is
+    timed through the oracle port on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    inp = cpu_sample_inputs()
+    for _ in range(args.warmup):
+        cpu_pass(inp, threads)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_pass(inp, threads)
+    dt = time.perf_counter() - t
+    U = 2 * L * edges(H, CPU_CROP_W)
+    value = U * args.steps / dt
+    sample = (f"oracle port of the reference recurrence (C++/OpenMP), per step one pass forward+backward on a "
+              f"{H}x{CPU_CROP_W}x{L} crop of the workload")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "stereo BP-Layer forward+backward, 376x1240x192, 3 iterations, FP32",
+                   "B": 1, "H": H, "W": W, "L": L, "iters": ITERS, "delta": DELTA, "cpu_crop_w": CPU_CROP_W},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def run_ncu_case(args):
+    """Small case for detailed ncu captures: one forward pass and one
+    reference-adjoint pass at 256x512x192 (cost 100 MB, messages 400 MB:
+    larger than L2, well under the capture size limit), inside a profiler
+    range."""
+    import torch
+    from bpl_gb300 import ops
+    import cases
+    dev = torch.device("cuda", 0)
+    h, w = 256, 512
+    g = cases.rng(3)
+    cost = torch.from_numpy(cases.random_cost(g, 1, h, w, L)).to(dev)
+    jump = torch.from_numpy(cases.stereo_taps(1, h, w, 0.1, 0.5)).to(dev)
+    edge = torch.from_numpy(cases.edge_weights(g, 1, h, w)).to(dev)
+    gin = torch.randn((1, 4, h, w, L), device=dev)
+    for it in range(2):
+        m = torch.zeros((1, 4, h, w, L), device=dev)
+        if it == 1:
+            torch.cuda.synchronize()
+            torch.cuda.profiler.start()
+        m, am, sc = ops.lbp_forward(ops.LBP_STEREO, cost, jump, edge, m, DELTA, argmin_dtype=torch.uint8)
+        ops.lbp_backward(ops.LBP_STEREO, jump, edge, gin, m, am, sc, copy_grad_messages=False)
+        torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"ncu_case": f"{h}x{w}x{L}", "updates_per_pass": L * edges(h, w)}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncu-case", action="store_true", help="small case for ncu captures")
+    args = ap.parse_args()
+    if args.ncu_case:
+        run_ncu_case(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

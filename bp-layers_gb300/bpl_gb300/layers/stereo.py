@@ -1,0 +1,229 @@
+"""Host-side mirror of the reference's stereo BP layer
+(ops/lbp_stereo/message_passing_op_cuda.py, ops/lbp_stereo/inference_op.py,
+ops/lbp_stereo/bp_op_cuda.py:130-210) on the GB300 kernels.
+
+Same classes, argument meaning and results.  Differences, all without effect
+on the values computed:
+  * argmin indices are kept as uint8 (L <= 256) or int16 inside the autograd
+    function instead of a float32 volume;
+  * no torch.cuda.empty_cache() per iteration, and the default offset tensor
+    is created on the device (the reference builds it on the host and copies
+    it every iteration, message_passing_op_cuda.py:157-158).
+"""
+from __future__ import annotations
+
+import torch
+import torch.nn as nn
+import torch.nn.functional as F
+
+from .. import ops
+
+
+class TemperatureSoftmin(nn.Module):
+    """softmin(x / T) along `dim` with a learnable temperature (corenet.py:106-113)."""
+
+    def __init__(self, dim, init_temp=1.0, device=None):
+        super().__init__()
+        self.T = nn.Parameter(torch.ones(1, device=device).float() * init_temp, requires_grad=True)
+        self.dim = dim
+
+    def forward(self, x):
+        return F.softmin(x / self.T, dim=self.dim)
+
+
+def pack_affinities(affinities, offset):
+    """(N,4,K,H,W) affinities [L2-, L2+, L1-, L1+, L3] (or [L1, L1, L2]) plus
+    offset (N,4,H,W) -> (N,4,K+3,H,W) jump taps [offset, L3, L2-, L1-, 0, L1+,
+    L2+, L3] with the reverse directions' +/- swapped
+    (message_passing_op_cuda.py:35-60)."""
+    N, D, K, H, W = affinities.shape
+    out = torch.zeros((N, D, K + 3, H, W), dtype=affinities.dtype, device=affinities.device)
+    out[:, :, 0] = offset
+    out[:, :, 1] = affinities[:, :, -1]
+    out[:, :, -1] = affinities[:, :, -1]
+    out[:, :, (K + 3) // 2] = 0.0
+    ic = 0
+    for i in range(2, (K + 3) // 2):
+        out[:, 0::2, i] = affinities[:, 0::2, ic]
+        out[:, 0::2, -i] = affinities[:, 0::2, ic + 1]
+        out[:, 1::2, i] = affinities[:, 1::2, ic + 1]
+        out[:, 1::2, -i] = affinities[:, 1::2, ic]
+        ic += 2
+    return out.contiguous()
+
+
+def unpack_affinity_grad(grad_taps):
+    """Inverse of pack_affinities for the gradient (message_passing_op_cuda.py:75-93).
+    Returns (grad_affinities (N,4,K,H,W), grad_offset (N,4,H,W))."""
+    N, D, Kp, H, W = grad_taps.shape
+    g = torch.zeros((N, D, Kp - 3, H, W), dtype=grad_taps.dtype, device=grad_taps.device)
+    g[:, :, -1] += grad_taps[:, :, 1]
+    g[:, :, -1] += grad_taps[:, :, -1]
+    ic = 0
+    for i in range(2, Kp // 2):
+        g[:, 0::2, ic] = grad_taps[:, 0::2, i]
+        g[:, 0::2, ic + 1] = grad_taps[:, 0::2, -i]
+        g[:, 1::2, ic + 1] = grad_taps[:, 1::2, i]
+        g[:, 1::2, ic] = grad_taps[:, 1::2, -i]
+        ic += 2
+    return g, grad_taps[:, :, 0]
+
+
+class LBPMinSumFunction(torch.autograd.Function):
+    """One LBP pass with the reference adjoint
+    (message_passing_op_cuda.py:22-93).  forward(cost, edge, messages, delta,
+    affinities, offset) -> messages (updated in place, like the reference)."""
+
+    @staticmethod
+    def forward(ctx, cost, edge, messages, delta, affinities, offset):
+        taps = pack_affinities(affinities, offset)
+        L = cost.shape[-1]
+        am_dtype = torch.uint8 if L <= 256 else torch.int16
+        messages, argmin, scale = ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta),
+                                                  argmin_dtype=am_dtype)
+        ctx.save_for_backward(cost, taps, edge, messages, argmin, scale)
+        return messages
+
+    @staticmethod
+    def backward(ctx, in_grad):
+        cost, taps, edge, messages, argmin, scale = ctx.saved_tensors
+        gc, gtaps, ge, gm = ops.lbp_backward(ops.LBP_STEREO, taps, edge, in_grad.contiguous(), messages, argmin,
+                                             scale, copy_grad_messages=False)
+        g_aff, g_off = unpack_affinity_grad(gtaps)
+        return gc, ge, gm, None, g_aff, g_off
+
+
+class MessagePassing(nn.Module):
+    """message_passing_op_cuda.py:95-177."""
+
+    @property
+    def L1(self):
+        return self._L1
+
+    @property
+    def L2(self):
+        return self._L2
+
+    def setL1L2(self, value_L1, value_L2):
+        if value_L1 > 0 and value_L2 > 0 and value_L1 <= value_L2:
+            self._L1 = value_L1
+            self._L2 = value_L2
+        elif value_L1 < 0 or value_L2 < 0:
+            raise ValueError("L1 or L2 is < 0!")
+        elif value_L1 > value_L2:
+            raise ValueError("L1 must be smaller than or equal L2!")
+
+    def __init__(self, device, max_iter, num_labels, delta, mode="min-sum"):
+        super().__init__()
+        self.device = device
+        self.max_iter = max_iter
+        if mode != "min-sum":
+            raise ValueError("Unknown message parsing mode " + mode)
+        self.mode = mode
+        self._L1 = nn.Parameter(torch.tensor(0.1, device=device), requires_grad=True)
+        self._L2 = nn.Parameter(torch.tensor(2.5, device=device), requires_grad=True)
+        self.softmin = TemperatureSoftmin(dim=3, init_temp=1.0, device=device)
+        self.delta = delta
+        self.rescaleT = None
+
+    def projectL1L2(self):
+        self.L2.data = torch.max(self.L1.data, self.L2.data)
+
+    def forward(self, prob_vol, edge_weights, affinities, offset, messages):
+        N, H, W, C = prob_vol.shape
+        dev = prob_vol.device
+        if edge_weights is None:
+            edge_weights = torch.ones((N, 4, H, W), device=dev)
+        if affinities is None:
+            if (self._L1 is not None) and (self._L2 is not None):
+                affinities = torch.zeros((N, 4, 3, H, W), dtype=torch.float, device=dev)
+                affinities[:, :, :2, :, :] = self._L1
+                affinities[:, :, 2, :, :] = self._L2
+        else:
+            if (self._L1 is not None and self._L2 is None) or (self._L1 is None and self._L2 is not None):
+                raise ValueError("L1 or L2 is None and affinities are not set!")
+        if offset is None:
+            offset = torch.zeros((N, 4, H, W), device=dev)
+        cost = -prob_vol
+        for _ in range(self.max_iter):
+            messages = LBPMinSumFunction.apply(cost, edge_weights, messages, self.delta, affinities, offset)
+        beliefs = messages.sum(dim=1) + cost
+        beliefs = self.softmin.forward(beliefs)
+        return beliefs, messages
+
+
+class Inference(nn.Module):
+    """ops/lbp_stereo/inference_op.py:5-97: wta / expectation / norm / raw / sub-exp."""
+
+    def __init__(self, device, mode="wta", mode_passing="min-sum"):
+        super().__init__()
+        if mode not in ("wta", "expectation", "norm", "raw", "sub-exp"):
+            raise ValueError("Unknown inference mode " + mode)
+        self.device = device
+        self.mode = mode
+        self.mode_passing = mode_passing
+
+    def forward(self, beliefs):
+        if self.mode == "wta":
+            return torch.argmax(beliefs, dim=3, keepdim=True)
+        if self.mode == "expectation":
+            bn = beliefs / beliefs.sum(dim=3, keepdim=True)
+            labels = torch.arange(beliefs.shape[3], device=beliefs.device, dtype=torch.float32).view(1, 1, 1, -1)
+            return (bn * labels).sum(dim=3, keepdim=True)
+        if self.mode == "norm":
+            return beliefs / beliefs.sum(dim=3, keepdim=True)
+        if self.mode == "raw":
+            return beliefs
+        return self.compute_sub_expectation(beliefs)
+
+    @staticmethod
+    def compute_sub_expectation(beliefs, support=3):
+        """+-support window around the argmax, renormalised expectation
+        (inference_op.py:53-97)."""
+        N, H, W, K = beliefs.shape
+        disp = beliefs.argmax(dim=-1).unsqueeze(-1)
+        win = torch.arange(-support, support + 1, device=beliefs.device) + disp
+        win = win.clamp(0, K - 1)
+        bw = torch.gather(beliefs, 3, win)
+        bw = bw / bw.sum(dim=-1, keepdim=True)
+        return torch.sum(bw * win, dim=-1, keepdim=True)
+
+
+def adjust_input_weights(weights, idx):
+    """bp_op_cuda.py:130-154: (N,2,H,W) x/y weights -> (N,4,H,W) per direction."""
+    if weights is None:
+        return None
+    out = torch.zeros((weights.shape[0], 4, weights.shape[2], weights.shape[3]), device=weights.device)
+    out[:, 0] = weights[:, 0]
+    out[:, 1, :, 1:] = weights[:, 0, :, :-1]
+    out[:, 2] = weights[:, 1]
+    out[:, 3, 1:, :] = weights[:, 1, :-1, :]
+    return out.contiguous()
+
+
+def adjust_input_affinities(affinities):
+    """bp_op_cuda.py:156-188: order constraint then shift to 4 directions."""
+    if affinities is None:
+        return None
+    a = affinities.clone()
+    a[:, :, 0] = torch.max(affinities[:, :, 0], affinities[:, :, 2])
+    a[:, :, 1] = torch.max(affinities[:, :, 1], affinities[:, :, 3])
+    a[:, :, 4] = torch.max(affinities[:, :, 4], torch.max(a[:, :, 0].clone(), a[:, :, 1].clone()))
+    s = torch.zeros((a.shape[0], a.shape[1] + 2, a.shape[2], a.shape[3], a.shape[4]), device=a.device)
+    s[:, 0] = a[:, 0]
+    s[:, 1, :, :, 1:] = a[:, 0, :, :, :-1]
+    s[:, 2] = a[:, 1]
+    s[:, 3, :, 1:, :] = a[:, 1, :, :-1, :]
+    return s.contiguous()
+
+
+def adjust_input_offsets(offsets):
+    """bp_op_cuda.py:190-209."""
+    if offsets is None:
+        return None
+    s = torch.zeros((offsets.shape[0], offsets.shape[1] + 2, offsets.shape[2], offsets.shape[3]), device=offsets.device)
+    s[:, 0] = offsets[:, 0]
+    s[:, 1, :, 1:] = -offsets[:, 0, :, :-1]
+    s[:, 2] = offsets[:, 1]
+    s[:, 3, 1:, :] = -offsets[:, 1, :-1, :]
+    return s.contiguous()

@@ -79,7 +79,97 @@ def lbp_forward(variant: int, cost: torch.Tensor, jump: torch.Tensor, edge: torc
             argmin = torch.zeros((B, 4, H, W, L), dtype=argmin_dtype, device=cost.device)
     if scale is None:
         scale = torch.zeros((B, 4, H, W), dtype=torch.float32, device=cost.device)
-    st = lib().bpl_lbp_forward(variant, _ptr(cost), _ptr(jump), _ptr(edge), _ptr(messages), _ptr(argmin), kind,
-                               _ptr(scale), B, H, W, L, Lv, jb, edge.shape[0], int(delta), _stream(cost))
+    st = _timed("lbp_forward", lambda: lib().bpl_lbp_forward(
+        variant, _ptr(cost), _ptr(jump), _ptr(edge), _ptr(messages), _ptr(argmin), kind, _ptr(scale),
+        B, H, W, L, Lv, jb, edge.shape[0], int(delta), _stream(cost)))
     check(st, "bpl_lbp_forward")
     return messages, argmin, scale
+
+
+def lbp_backward_workspace_bytes(B: int, H: int, W: int, L: int) -> int:
+    return int(lib().bpl_lbp_backward_workspace_size(B, H, W, L))
+
+
+def lbp_backward(variant: int, jump, edge: torch.Tensor, in_grad: torch.Tensor, messages: torch.Tensor,
+                 argmin: torch.Tensor, scale: torch.Tensor, workspace: torch.Tensor | None = None,
+                 copy_grad_messages: bool = True):
+    """Reference adjoint of one LBP pass.
+
+    Returns (grad_cost, grad_jump, grad_edge, grad_messages).  grad_messages
+    is in_grad (copied unless copy_grad_messages=False), grad_edge is None
+    for the pixel-pairwise variant.  `workspace` (uint8, at least
+    lbp_backward_workspace_bytes) may be passed to avoid allocating it.
+    """
+    _check_input("in_grad", in_grad, dim=5)
+    _check_input("messages", messages, dim=5)
+    _check_input("scale", scale, dim=4)
+    _check_input("edge", edge, dim=4)
+    _check_input("argmin", argmin, dtype=None, dim=5)
+    B, _, H, W, L = messages.shape
+    if tuple(in_grad.shape) != tuple(messages.shape) or tuple(argmin.shape) != tuple(messages.shape):
+        raise BplError("in_grad/argmin must have the messages' shape")
+    kind = _ARGMIN_KIND.get(argmin.dtype)
+    if kind is None:
+        raise BplError(f"argmin dtype {argmin.dtype} not supported")
+    dev = messages.device
+    Lv, jb = 0, 1
+    if variant == LBP_STEREO:
+        _check_input("jump", jump, dim=5)
+        Lv, jb = jump.shape[2], jump.shape[0]
+        grad_jump = torch.empty((jb, 4, Lv, H, W), dtype=torch.float32, device=dev)
+    elif variant == LBP_SEM_GLOBAL:
+        _check_input("jump", jump, dim=4)
+        grad_jump = torch.empty((B, 4, L, L), dtype=torch.float32, device=dev)
+    else:
+        grad_jump = torch.empty((4, H, W, L, L), dtype=torch.float32, device=dev)
+    grad_cost = torch.empty((B, H, W, L), dtype=torch.float32, device=dev)
+    grad_edge = None if variant == LBP_SEM_PIXEL else torch.empty(tuple(edge.shape), dtype=torch.float32, device=dev)
+    need = lbp_backward_workspace_bytes(B, H, W, L)
+    if workspace is None or workspace.numel() * workspace.element_size() < need:
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    st = _timed("lbp_backward", lambda: lib().bpl_lbp_backward(
+        variant, _ptr(jump) if variant != LBP_SEM_PIXEL else None, _ptr(edge), _ptr(in_grad),
+        _ptr(messages), _ptr(argmin), kind, _ptr(scale), _ptr(grad_cost), _ptr(grad_jump),
+        _ptr(grad_edge), _ptr(workspace), workspace.numel() * workspace.element_size(),
+        B, H, W, L, Lv, jb, edge.shape[0], _stream(messages)))
+    check(st, "bpl_lbp_backward")
+    grad_messages = in_grad.clone() if copy_grad_messages else in_grad
+    return grad_cost, grad_jump, grad_edge, grad_messages
+
+
+# ---------------------------------------------------------------------------
+# Per-op CUDA-event timing (tracing).  When enabled, every C-ABI call made
+# through this module records a start/end event pair on the stream it
+# launches on; `timing_report()` returns {op: [ms, ...]}.
+_timing = None
+
+
+class timing:
+    """Context manager: with ops.timing() as t: ...; then t.report()."""
+
+    def __enter__(self):
+        global _timing
+        self.events = {}
+        _timing = self.events
+        return self
+
+    def __exit__(self, *exc):
+        global _timing
+        _timing = None
+        return False
+
+    def report(self):
+        torch.cuda.synchronize()
+        return {k: [a.elapsed_time(b) for a, b in v] for k, v in self.events.items()}
+
+
+def _timed(name, fn):
+    if _timing is None:
+        return fn()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    r = fn()
+    b.record()
+    _timing.setdefault(name, []).append((a, b))
+    return r

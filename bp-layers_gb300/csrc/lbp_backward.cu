@@ -1,0 +1,74 @@
+// C-ABI entry of the LBP reference adjoint (argument checks, output
+// zero-fill, dispatch).
+#include "lbp_backward.cuh"
+
+using namespace bpl;
+
+extern "C" size_t bpl_lbp_backward_workspace_size(int B, int H, int W, int L) {
+  if (B < 1 || H < 1 || W < 1 || L < 1) return 0;
+  return static_cast<size_t>(B) * 2 * H * W * L * sizeof(float);
+}
+
+extern "C" int bpl_lbp_backward(int variant, const float* jump, const float* edge, const float* in_grad,
+                                const float* messages, const void* argmin, int argmin_kind,
+                                const float* scale, float* grad_cost, float* grad_jump, float* grad_edge,
+                                void* workspace, size_t workspace_bytes, int B, int H, int W, int L,
+                                int Lv, int jump_batch, int edge_batch, void* stream) {
+  BPL_REQUIRE(variant >= 0 && variant <= 2, "lbp_backward: unknown variant %d", variant);
+  BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1, "lbp_backward: bad shape B=%d H=%d W=%d", B, H, W);
+  BPL_REQUIRE(H <= 65535 && W <= 65535, "lbp_backward: H and W must be <= 65535");
+  BPL_REQUIRE(L >= 1 && L <= 1024, "lbp_backward: L=%d outside [1, 1024]", L);
+  BPL_REQUIRE(edge && in_grad && messages && argmin && scale && grad_cost && grad_jump,
+              "lbp_backward: null pointer");
+  BPL_REQUIRE(variant == BPL_LBP_SEM_PIXEL || (jump && grad_edge), "lbp_backward: null jump/grad_edge");
+  BPL_REQUIRE(argmin_kind >= BPL_ARGMIN_F32 && argmin_kind <= BPL_ARGMIN_U16, "lbp_backward: bad argmin kind");
+  BPL_REQUIRE(edge_batch == 1 || edge_batch == B, "lbp_backward: edge batch %d must be 1 or B", edge_batch);
+  BPL_REQUIRE(workspace && workspace_bytes >= bpl_lbp_backward_workspace_size(B, H, W, L),
+              "lbp_backward: workspace of %zu bytes needed", bpl_lbp_backward_workspace_size(B, H, W, L));
+  if (variant == BPL_LBP_STEREO) {
+    BPL_REQUIRE(Lv >= 2 && Lv <= 16, "lbp_backward: Lv=%d outside [2, 16]", Lv);
+    BPL_REQUIRE(jump_batch == 1 || jump_batch == B, "lbp_backward: jump batch %d must be 1 or B", jump_batch);
+  }
+  if (variant == BPL_LBP_SEM_PIXEL) BPL_REQUIRE(L <= 96, "lbp_backward: pixel-pairwise variant supports L <= 96");
+
+  cudaStream_t s = as_stream(stream);
+  const int64_t HW = static_cast<int64_t>(H) * W;
+  size_t gj_elems;
+  if (variant == BPL_LBP_STEREO) gj_elems = static_cast<size_t>(jump_batch) * 4 * Lv * HW;
+  else if (variant == BPL_LBP_SEM_GLOBAL) gj_elems = static_cast<size_t>(B) * 4 * L * L;
+  else gj_elems = static_cast<size_t>(4) * HW * L * L;
+  BPL_CUDA_TRY(cudaMemsetAsync(grad_cost, 0, sizeof(float) * B * HW * L, s), "lbp_backward: memset");
+  BPL_CUDA_TRY(cudaMemsetAsync(grad_jump, 0, sizeof(float) * gj_elems, s), "lbp_backward: memset");
+  if (grad_edge)
+    BPL_CUDA_TRY(cudaMemsetAsync(grad_edge, 0, sizeof(float) * edge_batch * 4 * HW, s), "lbp_backward: memset");
+
+  BwdArgs a{};
+  a.jump = jump;
+  a.edge = edge;
+  a.in_grad = in_grad;
+  a.msgs = messages;
+  a.argmin = argmin;
+  a.scale = scale;
+  a.grad_cost = grad_cost;
+  a.grad_jump = grad_jump;
+  a.grad_edge = grad_edge;
+  a.saved = static_cast<float*>(workspace);
+  a.B = B;
+  a.H = H;
+  a.W = W;
+  a.L = L;
+  a.Lv = (variant == BPL_LBP_STEREO) ? Lv : 0;
+  a.jb = jump_batch;
+  a.eb = edge_batch;
+  a.argmin_kind = argmin_kind;
+  a.lrow = bwd::a4(L);
+  a.vec4 = (L % 4 == 0) ? 1 : 0;
+  const int am_size = (argmin_kind == BPL_ARGMIN_U8) ? 1 : (argmin_kind == BPL_ARGMIN_U16 ? 2 : 4);
+  a.am_bulk = (a.vec4 && (L * am_size) % 16 == 0) ? 1 : 0;
+  a.ns = kBwdRingCpAsync;
+  switch (variant) {
+    case BPL_LBP_STEREO: return lbp_backward_stereo(a, s);
+    case BPL_LBP_SEM_GLOBAL: return lbp_backward_sem_global(a, s);
+    default: return lbp_backward_sem_pixel(a, s);
+  }
+}

@@ -1,0 +1,520 @@
+// Reference adjoint of the min-sum LBP pass for sm_103a (kernel template;
+// instantiated per pairwise variant in lbp_backward_*.cu).
+//
+// Reference semantics: ops/lbp_stereo/src/lbp_min_sum_kernel.cu:215-417
+// (kernel) and :513-621 (host loops: per batch item, reversed sweeps DOWN,
+// UP, LEFT, RIGHT, one launch plus an at::zeros scratch allocation per
+// column/row).  What the reference computes at a backward step (sender p,
+// receiver q, message slot db at q, forward direction fd = db^1), per
+// receiver label c:
+//   add_hor = J^T in_grad[q] + J^T acc_HOR         (LSE Jacobian, :328-369)
+//   add_up  = saved_UP[q] + acc_UP,  add_down = saved_DOWN[q] + acc_DOWN
+//             (horizontal sweeps only, no Jacobian, :380-386)
+//   s* = argmin[q][c]
+//   grad_cost[p][s*] += add_hor + add_up + add_down
+//   grad_jump[fd][tap(c - s*)][p] += w * (...), grad_edge[fd][p] += f(c,s*) * (...)
+//   acc_X_new[s*] += add_X;  saved_db[p] = acc_HOR_new (:404-416)
+// and grad_messages = in_grad (:534-536).
+//
+// GB300 design: one warp walks one scanline of one backward sweep, the
+// accumulators acc_HOR/UP/DOWN stay in registers, the scatter "by argmin"
+// goes through per-warp shared-memory rows with shared atomics, and the two
+// sweeps of each orientation run concurrently (DOWN+UP, then LEFT+RIGHT):
+// 2 launches per backward instead of 2(W-1)+2(H-1).  The J^T product is taken
+// in O(L) as g_c - p_c * sum(g) instead of the reference's O(L^2) loop.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "bpl_device.cuh"
+#include "bpl_internal.h"
+
+namespace bpl {
+
+struct BwdArgs {
+  const float* jump;
+  const float* edge;
+  const float* in_grad;
+  const float* msgs;
+  const void* argmin;
+  const float* scale;
+  float* grad_cost;
+  float* grad_jump;
+  float* grad_edge;
+  float* saved;  // workspace (B,2,H,W,L): slot 0 = UP chain, slot 1 = DOWN chain
+  int B, H, W, L, Lv, jb, eb;
+  int argmin_kind;
+  int phase;  // 0: DOWN+UP over columns, 1: LEFT+RIGHT over rows
+  int nchains;
+  int ns;
+  int lrow;
+  int vec4;     // float rows are 16-byte sized: bulk copies
+  int am_bulk;  // the argmin row is 16-byte sized too: staged with the floats
+};
+
+constexpr int kBwdRingCpAsync = 4;
+
+namespace bwd {
+
+__host__ __device__ inline int a4(int v) { return (v + 3) & ~3; }
+
+// rows per stage: messages, in_grad, saved UP, saved DOWN (floats) and the
+// argmin row (up to 4 bytes per label)
+__host__ __device__ inline int stage_floats(int lrow) { return 5 * lrow; }
+
+__host__ __device__ inline int tile_floats(int Lv) { return a4(2 * (Lv + 2) * 33); }
+
+__host__ __device__ inline int warp_smem_floats(int K, int ns, int lrow, int Lv, int L, int variant) {
+  const int ring = ns * stage_floats(lrow);
+  const int bars = 2 * a4(ns);
+  const int rows = 3 * 32 * K;                      // scatter rows of acc HOR/UP/DOWN
+  const int jacc = (variant == BPL_LBP_SEM_GLOBAL) ? a4(L * L) : 0;
+  return a4(ring) + bars + rows + jacc + tile_floats(Lv);
+}
+
+struct Smem {
+  float* ring;
+  uint64_t* bars;
+  float* rows;  // [3][32K]
+  float* jacc;  // [L*L] (semantic global)
+  float* tile;  // [2][Lv+2][33]: taps, edge weight, scale
+};
+
+template <int K>
+__device__ __forceinline__ Smem carve(float* base, const BwdArgs& a, int variant) {
+  Smem s;
+  s.ring = base;
+  float* p = base + a4(a.ns * stage_floats(a.lrow));
+  s.bars = reinterpret_cast<uint64_t*>(p);
+  p += 2 * a4(a.ns);
+  s.rows = p;
+  p += 3 * 32 * K;
+  s.jacc = p;
+  if (variant == BPL_LBP_SEM_GLOBAL) p += a4(a.L * a.L);
+  s.tile = p;
+  return s;
+}
+
+struct Chain {
+  int n, db, fixed, len;
+};
+
+// sender coordinate along the chain at step k
+__device__ __forceinline__ int sender(const Chain& c, int k) {
+  switch (c.db) {
+    case DOWN: return 1 + k;             // undoes the UP sweep
+    case UP: return c.len - 2 - k;       // undoes DOWN
+    case LEFT: return c.len - 2 - k;     // undoes RIGHT
+    default: return 1 + k;               // RIGHT: undoes LEFT
+  }
+}
+
+__device__ __forceinline__ int recv_delta(int db) {
+  // receiver coordinate - sender coordinate
+  return (db == DOWN || db == RIGHT) ? -1 : 1;
+}
+
+__device__ __forceinline__ int64_t pixel(const BwdArgs& a, const Chain& c, int v) {
+  const int y = (a.phase == 0) ? v : c.fixed;
+  const int x = (a.phase == 0) ? c.fixed : v;
+  return static_cast<int64_t>(y) * a.W + x;  // within image
+}
+
+}  // namespace bwd
+
+template <int K, int VARIANT>
+__global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
+  using namespace bwd;
+  extern __shared__ __align__(16) float smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int chain_id = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (chain_id >= a.nchains) return;
+
+  const int per_warp = warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, VARIANT);
+  Smem sm = carve<K>(smem + static_cast<int64_t>(wib) * per_warp, a, VARIANT);
+
+  const int L = a.L;
+  const int64_t HW = static_cast<int64_t>(a.H) * a.W;
+  Chain c;
+  const int r = chain_id >> 1;
+  if (a.phase == 0) {
+    c.db = (chain_id & 1) ? UP : DOWN;
+    c.n = r / a.W;
+    c.fixed = r % a.W;
+    c.len = a.H;
+  } else {
+    c.db = (chain_id & 1) ? RIGHT : LEFT;
+    c.n = r / a.H;
+    c.fixed = r % a.H;
+    c.len = a.W;
+  }
+  const int fd = c.db ^ 1;
+  const int nsteps = c.len - 1;
+  const bool cross = (a.phase == 1);
+  const bool stereo = (VARIANT == BPL_LBP_STEREO);
+  const int nj = (a.jb == 1) ? 0 : c.n;
+  const int ne = (a.eb == 1) ? 0 : c.n;
+
+  // saved rows never written by a sender are read as zero by the horizontal
+  // sweeps: the DOWN chain's row 0 and the UP chain's row H-1
+  if (a.phase == 0) {
+    const int v0 = (c.db == DOWN) ? 0 : (a.H - 1);
+    float* dst = a.saved + ((static_cast<int64_t>(c.n) * 2 + (c.db == UP ? 0 : 1)) * HW + pixel(a, c, v0)) * L;
+    for (int t = lane; t < L; t += 32) dst[t] = 0.0f;
+  }
+  if (nsteps <= 0) return;
+
+  // zero scatter rows / accumulators
+  for (int t = lane; t < 3 * 32 * K; t += 32) sm.rows[t] = 0.0f;
+  if (VARIANT == BPL_LBP_SEM_GLOBAL)
+    for (int t = lane; t < L * L; t += 32) sm.jacc[t] = 0.0f;
+
+  const int rd = recv_delta(c.db);
+  const uint32_t am_size = (a.argmin_kind == BPL_ARGMIN_U8) ? 1u : (a.argmin_kind == BPL_ARGMIN_U16 ? 2u : 4u);
+  auto issue = [&](int k) {
+    const int st = k % a.ns;
+    float* dst = sm.ring + static_cast<int64_t>(st) * stage_floats(a.lrow);
+    const int64_t q = pixel(a, c, sender(c, k) + rd);
+    const int64_t mo = ((static_cast<int64_t>(c.n) * 4 + c.db) * HW + q) * L;
+    const float* s0 = a.msgs + mo;
+    const float* s1 = a.in_grad + mo;
+    const float* s2 = a.saved + ((static_cast<int64_t>(c.n) * 2 + 0) * HW + q) * L;
+    const float* s3 = a.saved + ((static_cast<int64_t>(c.n) * 2 + 1) * HW + q) * L;
+    if (a.vec4) {
+      if (lane == 0) {
+        const uint32_t rb = static_cast<uint32_t>(L) * 4u;
+        const uint32_t ab = a.am_bulk ? static_cast<uint32_t>(L) * am_size : 0u;
+        fence_proxy_async();
+        mbar_arrive_expect_tx(&sm.bars[st], (cross ? 4u : 2u) * rb + ab);
+        bulk_g2s(dst, s0, rb, &sm.bars[st]);
+        bulk_g2s(dst + a.lrow, s1, rb, &sm.bars[st]);
+        if (cross) {
+          bulk_g2s(dst + 2 * a.lrow, s2, rb, &sm.bars[st]);
+          bulk_g2s(dst + 3 * a.lrow, s3, rb, &sm.bars[st]);
+        }
+        if (a.am_bulk)
+          bulk_g2s(dst + 4 * a.lrow, static_cast<const uint8_t*>(a.argmin) + mo * am_size, ab, &sm.bars[st]);
+      }
+    } else {
+      for (int t = lane; t < L; t += 32) {
+        cp_async4(dst + t, s0 + t);
+        cp_async4(dst + a.lrow + t, s1 + t);
+        if (cross) {
+          cp_async4(dst + 2 * a.lrow + t, s2 + t);
+          cp_async4(dst + 3 * a.lrow + t, s3 + t);
+        }
+      }
+    }
+  };
+
+  // per-step tile: stereo taps (Lv rows), edge weight (row Lv), scale (row Lv+1)
+  const int trow = a.Lv + 2;
+  auto load_tile_regs = [&](int b, float (&rg)[18]) {
+    const int k = 32 * b + lane;
+    if (k >= nsteps) return;
+    const int64_t p = pixel(a, c, sender(c, k));
+    const int64_t q = pixel(a, c, sender(c, k) + rd);
+    rg[a.Lv] = __ldg(a.edge + (static_cast<int64_t>(ne) * 4 + fd) * HW + p);
+    rg[a.Lv + 1] = __ldg(a.scale + (static_cast<int64_t>(c.n) * 4 + c.db) * HW + q);
+    if (stereo) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        if (j < a.Lv) rg[j] = __ldg(a.jump + ((static_cast<int64_t>(nj) * 4 + fd) * a.Lv + j) * HW + p);
+    }
+  };
+  auto store_tile = [&](float* tile, const float (&rg)[18]) {
+#pragma unroll
+    for (int j = 0; j < 18; ++j)
+      if (j < trow) tile[j * 33 + lane] = rg[j];
+  };
+
+  if (a.vec4 && lane == 0) {
+    for (int s = 0; s < a.ns; ++s) mbar_init(&sm.bars[s], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  for (int k = 0; k < a.ns; ++k) {
+    if (k < nsteps) issue(k);
+    if (!a.vec4) cp_async_commit();
+  }
+  float rg[18];
+#pragma unroll
+  for (int j = 0; j < 18; ++j) rg[j] = 0.0f;
+  load_tile_regs(0, rg);
+  store_tile(sm.tile, rg);
+  if (nsteps > 32) load_tile_regs(1, rg);
+  __syncwarp();
+
+  float accH[K], accU[K], accD[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) accH[k] = accU[k] = accD[k] = 0.0f;
+  float* rowH = sm.rows;
+  float* rowU = sm.rows + 32 * K;
+  float* rowD = sm.rows + 64 * K;
+
+  bool failed = false;
+  for (int k = 0; k < nsteps; ++k) {
+    const int st = k % a.ns;
+    const int j = k & 31;
+    const int b = k >> 5;
+    const float* tile = sm.tile + (b & 1) * (trow * 33);
+    const float* stg = sm.ring + static_cast<int64_t>(st) * stage_floats(a.lrow);
+    const int ys = sender(c, k);
+    const int64_t p = pixel(a, c, ys);
+    const int64_t q = pixel(a, c, ys + rd);
+    const int64_t mo = ((static_cast<int64_t>(c.n) * 4 + c.db) * HW + q) * L;
+
+    if (a.vec4) {
+      const bool ok = mbar_wait_bounded(&sm.bars[st], static_cast<uint32_t>((k / a.ns) & 1));
+      if (!__all_sync(FULL, ok)) { failed = true; break; }
+    } else {
+      cp_async_wait<kBwdRingCpAsync - 1>();
+      __syncwarp();
+    }
+
+    const float w = tile[a.Lv * 33 + j];
+    float g[K], pr[K], sU[K], sD[K];
+    int am[K];
+    float sg = 0.0f, sa = 0.0f;
+    const void* amrow = a.am_bulk ? static_cast<const void*>(stg + 4 * a.lrow)
+                                  : static_cast<const void*>(static_cast<const uint8_t*>(a.argmin) + mo * am_size);
+#pragma unroll
+    for (int kk = 0; kk < K; ++kk) {
+      const int t = lane + 32 * kk;
+      g[kk] = 0.0f; pr[kk] = 0.0f; sU[kk] = 0.0f; sD[kk] = 0.0f; am[kk] = 0;
+      if (t < L) {
+        g[kk] = stg[a.lrow + t];
+        if (cross) {
+          sU[kk] = stg[2 * a.lrow + t];
+          sD[kk] = stg[3 * a.lrow + t];
+        }
+        // exp(m + log S) / S of the reference (:328-341) is exp(m) for a
+        // normalised message m = m_raw - log S
+        pr[kk] = expf(stg[t]);
+        if (a.argmin_kind == BPL_ARGMIN_U8) am[kk] = static_cast<const uint8_t*>(amrow)[t];
+        else if (a.argmin_kind == BPL_ARGMIN_U16) am[kk] = static_cast<const uint16_t*>(amrow)[t];
+        else am[kk] = static_cast<int>(static_cast<const float*>(amrow)[t]);
+        sg += g[kk];
+        sa += accH[kk];
+      }
+    }
+    // stage consumed: refill with step k + ns
+    __syncwarp();
+    if (k + a.ns < nsteps) issue(k + a.ns);
+    if (!a.vec4) cp_async_commit();
+
+    sg = warp_sum(sg);
+    sa = warp_sum(sa);
+    float addH[K], addU[K], addD[K];
+#pragma unroll
+    for (int kk = 0; kk < K; ++kk) {
+      addH[kk] = (g[kk] - pr[kk] * sg) + (accH[kk] - pr[kk] * sa);
+      addU[kk] = cross ? sU[kk] + accU[kk] : 0.0f;
+      addD[kk] = cross ? sD[kk] + accD[kk] : 0.0f;
+    }
+
+    // Scatter by argmin.  Most labels share one argmin (the label of the
+    // global minimum of h, for every label farther than the truncation window
+    // from it): that group is summed with warp shuffles, the few others go
+    // through shared-memory atomics with little contention.
+    int amL = 0;
+#pragma unroll
+    for (int kk = 0; kk < K; ++kk)
+      if (kk == ((L - 1) >> 5)) amL = am[kk];
+    const int g0 = __shfl_sync(FULL, am[0], 0);
+    const int gL = __shfl_sync(FULL, amL, (L - 1) & 31);
+    int c0 = 0, cL = 0;
+#pragma unroll
+    for (int kk = 0; kk < K; ++kk) {
+      const bool v = lane + 32 * kk < L;
+      c0 += __popc(__ballot_sync(FULL, v && am[kk] == g0));
+      cL += __popc(__ballot_sync(FULL, v && am[kk] == gL));
+    }
+    const int gd = (c0 >= cL) ? g0 : gL;
+    float dh = 0.0f, du = 0.0f, dd = 0.0f;
+#pragma unroll
+    for (int kk = 0; kk < K; ++kk) {
+      if (lane + 32 * kk < L) {
+        if (am[kk] == gd) {
+          dh += addH[kk];
+          du += addU[kk];
+          dd += addD[kk];
+        } else {
+          atomicAdd(&rowH[am[kk]], addH[kk]);
+          if (cross) {
+            atomicAdd(&rowU[am[kk]], addU[kk]);
+            atomicAdd(&rowD[am[kk]], addD[kk]);
+          }
+        }
+      }
+    }
+    dh = warp_sum(dh);
+    if (cross) {
+      du = warp_sum(du);
+      dd = warp_sum(dd);
+    }
+    if (lane == 0) {
+      rowH[gd] += dh;  // no other lane touches label gd
+      if (cross) {
+        rowU[gd] += du;
+        rowD[gd] += dd;
+      }
+    }
+
+    // pairwise and edge gradients
+    if (stereo) {
+      // per-tap sums of the total contribution; tap index clamp(Lv/2 + t - s*)
+      float bins[16];
+#pragma unroll
+      for (int bb = 0; bb < 16; ++bb) bins[bb] = 0.0f;
+#pragma unroll
+      for (int kk = 0; kk < K; ++kk) {
+        const int t = lane + 32 * kk;
+        if (t < L) {
+          const float tot = (addH[kk] + addU[kk]) + addD[kk];
+          const int ti = max(1, min(a.Lv - 1, a.Lv / 2 + (t - am[kk])));
+#pragma unroll
+          for (int bb = 1; bb < 16; ++bb)
+            if (bb < a.Lv) bins[bb] += (ti == bb) ? tot : 0.0f;
+        }
+      }
+      float ge = 0.0f;
+#pragma unroll
+      for (int bb = 1; bb < 16; ++bb) {
+        if (bb < a.Lv) {
+          const float v = warp_sum(bins[bb]);
+          ge += tile[bb * 33 + j] * v;
+          if (lane == bb && v != 0.0f)
+            atomicAdd(a.grad_jump + ((static_cast<int64_t>(nj) * 4 + fd) * a.Lv + bb) * HW + p, w * v);
+        }
+      }
+      if (lane == 0 && ge != 0.0f) atomicAdd(a.grad_edge + (static_cast<int64_t>(ne) * 4 + fd) * HW + p, ge);
+    } else {
+      float ge = 0.0f;
+#pragma unroll
+      for (int kk = 0; kk < K; ++kk) {
+        const int t = lane + 32 * kk;
+        if (t < L) {
+          const float tot = (addH[kk] + addU[kk]) + addD[kk];
+          const int s = am[kk];
+          if (VARIANT == BPL_LBP_SEM_GLOBAL) {
+            sm.jacc[s * L + t] += w * tot;  // distinct t per lane: no conflict
+            ge += __ldg(a.jump + (static_cast<int64_t>(fd) * L + s) * L + t) * tot;
+          } else {
+            // (4,H,W,L,L) has no batch axis: batch items accumulate
+            atomicAdd(a.grad_jump + ((static_cast<int64_t>(fd) * HW + p) * L + s) * L + t, w * tot);
+          }
+        }
+      }
+      if (VARIANT == BPL_LBP_SEM_GLOBAL) {
+        ge = warp_sum(ge);
+        if (lane == 0) atomicAdd(a.grad_edge + (static_cast<int64_t>(ne) * 4 + fd) * HW + p, ge);
+      }
+    }
+    __syncwarp();
+
+    // read back the chain accumulators (and clear the rows for the next
+    // step); grad_cost[p][s] receives rowH + rowU + rowD
+    float* gc = a.grad_cost + (static_cast<int64_t>(c.n) * HW + p) * L;
+#pragma unroll
+    for (int kk = 0; kk < K; ++kk) {
+      const int t = lane + 32 * kk;
+      if (t < L) {
+        accH[kk] = rowH[t];
+        rowH[t] = 0.0f;
+        float v = accH[kk];
+        if (cross) {
+          accU[kk] = rowU[t];
+          accD[kk] = rowD[t];
+          rowU[t] = 0.0f;
+          rowD[t] = 0.0f;
+          v = (v + accU[kk]) + accD[kk];
+        }
+        if (v != 0.0f) atomicAdd(gc + t, v);
+        if (a.phase == 0)
+          a.saved[((static_cast<int64_t>(c.n) * 2 + (c.db == UP ? 0 : 1)) * HW + p) * L + t] = accH[kk];
+      }
+    }
+
+    if (j == 31 || k == nsteps - 1) {
+      __syncwarp();
+      if (32 * (b + 1) < nsteps) {
+        store_tile(sm.tile + ((b + 1) & 1) * (trow * 33), rg);
+        if (32 * (b + 2) < nsteps) load_tile_regs(b + 2, rg);
+      }
+    }
+    __syncwarp();
+  }
+
+  if (VARIANT == BPL_LBP_SEM_GLOBAL) {
+    // global pairwise gradient: summed over batch items into item 0, as the
+    // reference does (ops/lbp_semantic_pw/src/lbp_min_sum_kernel.cu:395-397)
+    __syncwarp();
+    for (int t = lane; t < L * L; t += 32) {
+      const float v = sm.jacc[t];
+      if (v != 0.0f) atomicAdd(a.grad_jump + static_cast<int64_t>(fd) * L * L + t, v);
+    }
+  }
+  if (failed && a.vec4 && lane == 0) {
+    for (int s = 0; s < a.ns; ++s)
+      if (!mbar_try_wait(&sm.bars[s], 0) && !mbar_try_wait(&sm.bars[s], 1))
+        (void)mbar_wait_bounded(&sm.bars[s], 0, 1u << 16);
+  }
+  if (!a.vec4) cp_async_wait<0>();
+}
+
+template <int K, int V>
+int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
+  BwdArgs a = a0;
+  const int per_warp = bwd::warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, V) * 4;
+  const int wpb = std::max(1, std::min(4, (200 * 1024) / per_warp));
+  const size_t smem = static_cast<size_t>(per_warp) * wpb;
+  auto kern = lbp_backward_kernel<K, V>;
+  if (smem > 48 * 1024) {
+    if (static_cast<int>(smem) > max_smem_optin())
+      return set_error(BPL_ERR_UNSUPPORTED, "lbp_backward: shared memory %zu exceeds device limit", smem);
+    BPL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+                 "cudaFuncSetAttribute");
+  }
+  for (int phase = 0; phase < 2; ++phase) {
+    a.phase = phase;
+    a.nchains = 2 * a.B * (phase == 0 ? a.W : a.H);
+    const int blocks = (a.nchains + wpb - 1) / wpb;
+    kern<<<blocks, 32 * wpb, smem, stream>>>(a);
+    BPL_CUDA_TRY(cudaGetLastError(), "lbp_backward launch");
+  }
+  return BPL_OK;
+}
+
+template <int V>
+int dispatch_bwd(const BwdArgs& a, cudaStream_t s) {
+  const int k = (a.L + 31) / 32;
+  if constexpr (V == BPL_LBP_SEM_PIXEL) {
+    if (k == 1) return launch_bwd_k<1, V>(a, s);
+    if (k == 2) return launch_bwd_k<2, V>(a, s);
+    return launch_bwd_k<3, V>(a, s);
+  }
+  switch (k) {
+    case 1: return launch_bwd_k<1, V>(a, s);
+    case 2: return launch_bwd_k<2, V>(a, s);
+    case 3: return launch_bwd_k<3, V>(a, s);
+    case 4: return launch_bwd_k<4, V>(a, s);
+    case 5: return launch_bwd_k<5, V>(a, s);
+    case 6: return launch_bwd_k<6, V>(a, s);
+    case 7: return launch_bwd_k<7, V>(a, s);
+    case 8: return launch_bwd_k<8, V>(a, s);
+    default:
+      if (k <= 12) return launch_bwd_k<12, V>(a, s);
+      if (k <= 16) return launch_bwd_k<16, V>(a, s);
+      if (k <= 24) return launch_bwd_k<24, V>(a, s);
+      return launch_bwd_k<32, V>(a, s);
+  }
+}
+
+int lbp_backward_stereo(const BwdArgs& a, cudaStream_t s);
+int lbp_backward_sem_global(const BwdArgs& a, cudaStream_t s);
+int lbp_backward_sem_pixel(const BwdArgs& a, cudaStream_t s);
+
+}  // namespace bpl

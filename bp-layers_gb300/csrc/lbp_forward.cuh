@@ -25,6 +25,7 @@
 
 #include <algorithm>
 
+#include "bpl_crmath.cuh"
 #include "bpl_device.cuh"
 #include "bpl_internal.h"
 
@@ -51,9 +52,20 @@ struct FwdArgs {
   int vec4;   // rows are 16-byte sized: use bulk copies
 };
 
-// exp/log of the message normalisation, evaluated as the reference does
-// (double precision, rounded to float: lbp_min_sum_kernel.cu:167, :180-181).
-__device__ __forceinline__ float norm_exp(float m) { return static_cast<float>(exp(static_cast<double>(m))); }
+// exp/log of the message normalisation with the reference's results
+// ((float)exp((double)m) and (float)log(max((double)sum, 1e-45)),
+// lbp_min_sum_kernel.cu:167, :180-181): correctly rounded float-float
+// evaluation, double precision only when the rounding is undecided.
+__device__ __forceinline__ float norm_exp(float m, const float* ehi, const float* elo) {
+  float y;
+  if (!crm::exp_fast(m, y, ehi, elo)) y = static_cast<float>(exp(static_cast<double>(m)));
+  return y;
+}
+__device__ __forceinline__ float norm_log(float sum) {
+  float y;
+  if (!crm::log_fast(sum, y)) y = static_cast<float>(log(fmax(static_cast<double>(sum), 1e-45)));
+  return y;
+}
 
 // Per-warp shared memory carve-up (all offsets in floats, 16-byte aligned).
 struct WarpSmem {
@@ -204,6 +216,13 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
 
   const int per_warp = warp_smem_floats(K, a.ns, a.lrow, a.lmat, a.Lv);
   WarpSmem sm = carve<K>(smem + static_cast<int64_t>(wib) * per_warp, a);
+  // exp table for lane-varying lookups: every warp writes the same values
+  __shared__ float s_ehi[64], s_elo[64];
+  s_ehi[lane] = crm::kTab.exp_hi[lane];
+  s_ehi[lane + 32] = crm::kTab.exp_hi[lane + 32];
+  s_elo[lane] = crm::kTab.exp_lo[lane];
+  s_elo[lane + 32] = crm::kTab.exp_lo[lane + 32];
+  __syncwarp();
 
   Chain c;
   const int r = chain_id >> 1;
@@ -400,10 +419,10 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
     // normalisation (lbp_min_sum_kernel.cu:166-181)
     float e[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) e[k] = (lane + 32 * k < L) ? norm_exp(msg[k]) : 0.0f;
+    for (int k = 0; k < K; ++k) e[k] = (lane + 32 * k < L) ? norm_exp(msg[k], s_ehi, s_elo) : 0.0f;
     const float sum = tree_sum<K>(e, L, lane);
     const double sum_exp = fmax(static_cast<double>(sum), 1e-45);
-    const float lse = static_cast<float>(log(sum_exp));
+    const float lse = norm_log(sum);
 
     // write the message at the receiver
     const int64_t pq = pix_index(a, c, i) + ((a.phase == 0) ? ((c.dir == RIGHT) ? 1 : -1)

@@ -85,6 +85,41 @@ int bpl_lbp_forward(int variant, const float* cost, const float* jump, const flo
                     float* messages, void* argmin, int argmin_kind, float* scale, int B, int H,
                     int W, int L, int Lv, int jump_batch, int edge_batch, int delta, void* stream);
 
+/* Bytes of device workspace bpl_lbp_backward needs: B*2*H*W*L floats (the
+ * vertical sweeps' chain gradients that the horizontal sweeps read; the
+ * reference allocates the same as saved_prev_grad_msg,
+ * ops/lbp_stereo/src/lbp_min_sum_kernel.cu:538). */
+size_t bpl_lbp_backward_workspace_size(int B, int H, int W, int L);
+
+/*
+ * Reference adjoint of one LBP pass ("backward_minsum").
+ * Replaces cuda::lbp_backward_min_sum
+ *   ops/lbp_stereo/src/lbp_min_sum_kernel.cu:513-621          (STEREO)
+ *   ops/lbp_semantic_pw/src/lbp_min_sum_kernel.cu:516-624      (SEM_GLOBAL)
+ *   ops/lbp_semantic_pw_pixel/src/lbp_min_sum_kernel.cu:512-620 (SEM_PIXEL)
+ * bound in Python as `backward_minsum` (ops/lbp_stereo/src/lbp.cpp:29-46).
+ *
+ * Inputs: in_grad (B,4,H,W,L) upstream gradient of the messages; messages,
+ * argmin (argmin_kind F32/U8/U16) and scale as returned by bpl_lbp_forward.
+ * Outputs (zero-filled by this call, then accumulated):
+ *   grad_cost (B,H,W,L);
+ *   grad_jump: STEREO (jump_batch,4,Lv,H,W); SEM_GLOBAL (B,4,L,L) with the
+ *     gradient of the shared matrix summed into batch item 0, like the
+ *     reference; SEM_PIXEL (4,H,W,L,L);
+ *   grad_edge (edge_batch,4,H,W) (NULL allowed for SEM_PIXEL, which has no
+ *     edge gradient in the reference).
+ * The message gradient of the reference op is in_grad itself (the caller
+ * copies it if it needs a distinct tensor).  jump may be NULL for SEM_PIXEL.
+ * workspace: device scratch of bpl_lbp_backward_workspace_size() bytes.
+ * Float atomics make the summation order, and so the last bits, vary from
+ * run to run, as in the reference.
+ */
+int bpl_lbp_backward(int variant, const float* jump, const float* edge, const float* in_grad,
+                     const float* messages, const void* argmin, int argmin_kind, const float* scale,
+                     float* grad_cost, float* grad_jump, float* grad_edge, void* workspace,
+                     size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
+                     int edge_batch, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -264,8 +264,7 @@ void lbp_forward(int variant, const T* cost, const T* jump, const T* edge, T* ms
 //   stereo  (B,4,Lv,H,W)   [reference allocates batch 1 and indexes by n]
 //   global  (B,4,L,L)      [reference writes batch 0 only, :395-397]
 //   pixel   (4,H,W,L,L)
-// Edge gradient: stereo (B,4,H,W); global writes batch 0 only (:400-402);
-// pixel has none.
+// Edge gradient: (B,4,H,W) per batch item; pixel has none.
 void lbp_backward_ref(int variant, const float* jump, const float* edge, const float* in_grad,
                       const float* msgs, const float* argmin, const float* scale, double* g_cost,
                       double* g_jump, double* g_edge, double* g_msgs, int B, int H, int W, int L,
@@ -341,8 +340,10 @@ void lbp_backward_ref(int variant, const float* jump, const float* edge, const f
               nacc[L + s] += add_u;
               nacc[2 * L + s] += add_d;
             }
-            if (variant == VAR_STEREO) g_edge[S.dir(n, fd, y, x)] += ge;
-            else if (variant == VAR_SEM_GLOBAL) g_edge[S.dir(0, fd, y, x)] += ge;
+            // per batch item (the reference writes batch 0 for the global
+            // variant, :400-402; identical at B=1, the only batch size its
+            // forward processes)
+            if (variant != VAR_SEM_PIXEL) g_edge[S.dir(n, fd, y, x)] += ge;
             acc.swap(nacc);
             double* sv = saved.data() + S.msg(n, db, y, x);
             for (int c = 0; c < L; ++c) sv[c] = acc[c];

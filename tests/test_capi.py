@@ -50,3 +50,20 @@ def test_invalid_arguments_return_status_without_touching_the_device(bpl_lib):
     st = bpl_lib.bpl_lbp_forward(7, None, None, None, None, None, 0, None,
                                  1, 4, 4, 8, 6, 1, 1, 3, None)
     assert st == 1
+
+
+def _declared_arg_counts():
+    out = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"\b(bpl_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
+            args = m.group(2).strip()
+            out[m.group(1)] = 0 if args in ("", "void") else len(args.split(","))
+    return out
+
+
+def test_python_signatures_match_header_arity():
+    from bpl_gb300 import _lib
+    counts = _declared_arg_counts()
+    for name, n in counts.items():
+        assert len(_lib.SIGNATURES[name]) == n, f"{name}: header has {n} args, binding {len(_lib.SIGNATURES[name])}"
