@@ -107,7 +107,7 @@ class ClockSampler:
                 "samples": len(sms), "reasons": sorted(reasons)}
 
 
-def synth_inputs(torch, dev, seed):
+def synth_inputs(torch, dev, seed, H=H, W=W):
     """Piecewise-planar stereo scene -> SAD (C=64, D=192) -> softmax -> prob volume."""
     import numpy as np
     import cases
@@ -336,22 +336,21 @@ def run_reference(args):
 
 
 def run_ncu_case(args):
-    """Small case for detailed ncu captures: one forward pass and one
-    reference-adjoint pass at 256x512x192 (cost 100 MB, messages 400 MB:
-    larger than L2, well under the capture size limit), inside a profiler
-    range."""
+    """Small case for detailed ncu captures: the second of two forward passes
+    and reference-adjoint passes at 256x512x192 on the synthetic scene (cost
+    100 MB, messages 400 MB: larger than L2, well under the capture size
+    limit), inside a profiler range."""
     import torch
     from bpl_gb300 import ops
     import cases
     dev = torch.device("cuda", 0)
     h, w = 256, 512
-    g = cases.rng(3)
-    cost = torch.from_numpy(cases.random_cost(g, 1, h, w, L)).to(dev)
+    prob, edge, _ = synth_inputs(torch, dev, 3, H=h, W=w)
+    cost = (-prob).contiguous()
     jump = torch.from_numpy(cases.stereo_taps(1, h, w, 0.1, 0.5)).to(dev)
-    edge = torch.from_numpy(cases.edge_weights(g, 1, h, w)).to(dev)
     gin = torch.randn((1, 4, h, w, L), device=dev)
+    m = torch.zeros((1, 4, h, w, L), device=dev)
     for it in range(2):
-        m = torch.zeros((1, 4, h, w, L), device=dev)
         if it == 1:
             torch.cuda.synchronize()
             torch.cuda.profiler.start()

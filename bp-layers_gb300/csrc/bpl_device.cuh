@@ -73,7 +73,9 @@ __device__ __forceinline__ void tree_argmin(float (&v)[K], int (&lab)[K], int L,
   out_l = __shfl_sync(FULL, l0, 0);
 }
 
-// Sum tree (lbp_min_sum_kernel.cu:170-177).  Returns the warp-uniform sum.
+// Sum tree (lbp_min_sum_kernel.cu:170-177) of non-negative values.  Returns
+// the warp-uniform sum.  Branch-free: a position that does not take part at a
+// level adds +0.0, which leaves a non-negative float unchanged.
 template <int K>
 __device__ __forceinline__ float tree_sum(float (&v)[K], int L, int lane) {
 #pragma unroll
@@ -82,15 +84,22 @@ __device__ __forceinline__ float tree_sum(float (&v)[K], int L, int lane) {
     for (int k = 0; k < m; ++k) {
       if (k + m < K) {
         const int t = lane + 32 * k;
-        if (t + 32 * m < L) v[k] = __fadd_rn(v[k], v[k + m]);
+        v[k] = __fadd_rn(v[k], (t + 32 * m < L) ? v[k + m] : 0.0f);
       }
     }
   }
   float v0 = v[0];
-  int s = (K > 1) ? 16 : (np2(L) / 2);
-  for (; s > 0; s >>= 1) {
-    const float o = __shfl_down_sync(FULL, v0, s);
-    if (lane < s && lane + s < L) v0 = __fadd_rn(v0, o);
+  if (K > 1) {
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+      const float o = __shfl_down_sync(FULL, v0, s);
+      v0 = __fadd_rn(v0, (lane < s) ? o : 0.0f);
+    }
+  } else {
+    for (int s = np2(L) / 2; s > 0; s >>= 1) {
+      const float o = __shfl_down_sync(FULL, v0, s);
+      v0 = __fadd_rn(v0, (lane < s && lane + s < L) ? o : 0.0f);
+    }
   }
   return __shfl_sync(FULL, v0, 0);
 }

@@ -123,7 +123,9 @@ __device__ __forceinline__ int64_t pixel(const BwdArgs& a, const Chain& c, int v
 
 }  // namespace bwd
 
-template <int K, int VARIANT>
+// LV: number of stereo jump taps when known at compile time (6 or 8), 16 for
+// any Lv <= 16 given at run time, 0 for the semantic variants.
+template <int K, int VARIANT, int LV>
 __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   using namespace bwd;
   extern __shared__ __align__(16) float smem[];
@@ -366,24 +368,26 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
     // pairwise and edge gradients
     if (stereo) {
       // per-tap sums of the total contribution; tap index clamp(Lv/2 + t - s*)
-      float bins[16];
+      constexpr int NB = (LV > 0) ? LV : 16;
+      const int lv = (LV == 6 || LV == 8) ? LV : a.Lv;
+      float bins[NB];
 #pragma unroll
-      for (int bb = 0; bb < 16; ++bb) bins[bb] = 0.0f;
+      for (int bb = 0; bb < NB; ++bb) bins[bb] = 0.0f;
 #pragma unroll
       for (int kk = 0; kk < K; ++kk) {
         const int t = lane + 32 * kk;
         if (t < L) {
           const float tot = (addH[kk] + addU[kk]) + addD[kk];
-          const int ti = max(1, min(a.Lv - 1, a.Lv / 2 + (t - am[kk])));
+          const int ti = max(1, min(lv - 1, lv / 2 + (t - am[kk])));
 #pragma unroll
-          for (int bb = 1; bb < 16; ++bb)
-            if (bb < a.Lv) bins[bb] += (ti == bb) ? tot : 0.0f;
+          for (int bb = 1; bb < NB; ++bb)
+            if (bb < lv) bins[bb] += (ti == bb) ? tot : 0.0f;
         }
       }
       float ge = 0.0f;
 #pragma unroll
-      for (int bb = 1; bb < 16; ++bb) {
-        if (bb < a.Lv) {
+      for (int bb = 1; bb < NB; ++bb) {
+        if (bb < lv) {
           const float v = warp_sum(bins[bb]);
           ge += tile[bb * 33 + j] * v;
           if (lane == bb && v != 0.0f)
@@ -465,13 +469,13 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   if (!a.vec4) cp_async_wait<0>();
 }
 
-template <int K, int V>
+template <int K, int V, int LV>
 int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
   BwdArgs a = a0;
   const int per_warp = bwd::warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, V) * 4;
   const int wpb = std::max(1, std::min(4, (200 * 1024) / per_warp));
   const size_t smem = static_cast<size_t>(per_warp) * wpb;
-  auto kern = lbp_backward_kernel<K, V>;
+  auto kern = lbp_backward_kernel<K, V, LV>;
   if (smem > 48 * 1024) {
     if (static_cast<int>(smem) > max_smem_optin())
       return set_error(BPL_ERR_UNSUPPORTED, "lbp_backward: shared memory %zu exceeds device limit", smem);
@@ -488,31 +492,33 @@ int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
   return BPL_OK;
 }
 
-template <int V>
+template <int V, int LV>
 int dispatch_bwd(const BwdArgs& a, cudaStream_t s) {
   const int k = (a.L + 31) / 32;
   if constexpr (V == BPL_LBP_SEM_PIXEL) {
-    if (k == 1) return launch_bwd_k<1, V>(a, s);
-    if (k == 2) return launch_bwd_k<2, V>(a, s);
-    return launch_bwd_k<3, V>(a, s);
+    if (k == 1) return launch_bwd_k<1, V, LV>(a, s);
+    if (k == 2) return launch_bwd_k<2, V, LV>(a, s);
+    return launch_bwd_k<3, V, LV>(a, s);
   }
   switch (k) {
-    case 1: return launch_bwd_k<1, V>(a, s);
-    case 2: return launch_bwd_k<2, V>(a, s);
-    case 3: return launch_bwd_k<3, V>(a, s);
-    case 4: return launch_bwd_k<4, V>(a, s);
-    case 5: return launch_bwd_k<5, V>(a, s);
-    case 6: return launch_bwd_k<6, V>(a, s);
-    case 7: return launch_bwd_k<7, V>(a, s);
-    case 8: return launch_bwd_k<8, V>(a, s);
+    case 1: return launch_bwd_k<1, V, LV>(a, s);
+    case 2: return launch_bwd_k<2, V, LV>(a, s);
+    case 3: return launch_bwd_k<3, V, LV>(a, s);
+    case 4: return launch_bwd_k<4, V, LV>(a, s);
+    case 5: return launch_bwd_k<5, V, LV>(a, s);
+    case 6: return launch_bwd_k<6, V, LV>(a, s);
+    case 7: return launch_bwd_k<7, V, LV>(a, s);
+    case 8: return launch_bwd_k<8, V, LV>(a, s);
     default:
-      if (k <= 12) return launch_bwd_k<12, V>(a, s);
-      if (k <= 16) return launch_bwd_k<16, V>(a, s);
-      if (k <= 24) return launch_bwd_k<24, V>(a, s);
-      return launch_bwd_k<32, V>(a, s);
+      if (k <= 12) return launch_bwd_k<12, V, LV>(a, s);
+      if (k <= 16) return launch_bwd_k<16, V, LV>(a, s);
+      if (k <= 24) return launch_bwd_k<24, V, LV>(a, s);
+      return launch_bwd_k<32, V, LV>(a, s);
   }
 }
 
+int lbp_backward_stereo_lv6(const BwdArgs& a, cudaStream_t s);
+int lbp_backward_stereo_lv8(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_stereo(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_sem_global(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_sem_pixel(const BwdArgs& a, cudaStream_t s);

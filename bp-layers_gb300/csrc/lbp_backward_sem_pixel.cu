@@ -2,5 +2,5 @@
 #include "lbp_backward.cuh"
 
 namespace bpl {
-int lbp_backward_sem_pixel(const BwdArgs& a, cudaStream_t s) { return dispatch_bwd<BPL_LBP_SEM_PIXEL>(a, s); }
+int lbp_backward_sem_pixel(const BwdArgs& a, cudaStream_t s) { return dispatch_bwd<BPL_LBP_SEM_PIXEL, 0>(a, s); }
 }  // namespace bpl

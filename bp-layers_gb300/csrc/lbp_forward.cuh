@@ -18,8 +18,10 @@
 //     cross-direction messages) are streamed into a per-warp shared-memory
 //     ring NS pixels ahead with TMA 1-D bulk copies (cp.async.bulk +
 //     mbarrier), or 4-byte cp.async when a row is not 16-byte sized.
-//   * Labels are spread over lanes (label = lane + 32k); min/argmin and the
-//     exp-sum follow the reference's reduction tree exactly (bpl_device.cuh).
+//   * Labels are spread over lanes (label = lane + 32k).  min/argmin and the
+//     exp-sum reproduce the reference's reduction tree (bpl_device.cuh); the
+//     exp/log of the normalisation are correctly rounded float evaluations
+//     equal to the reference's double-precision ones (bpl_crmath.cuh).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -34,6 +36,15 @@ namespace bpl {
 // ring depth when rows are fetched with 4-byte cp.async (compile-time for
 // cp.async.wait_group)
 constexpr int kRingCpAsync = 4;
+
+// largest truncation half-width served by the unrolled zero-offset window
+constexpr int kFastDelta = 4;
+// +inf padding on each side of the per-warp h row
+constexpr int kHsPad = 4;
+// A phase whose scanlines number fewer than this many per SM splits each
+// scanline's labels over several warps (0: never; the split pays only when
+// the per-label work dominates the per-step reductions).
+constexpr int kSplitChainsPerSm = 0;
 
 struct FwdArgs {
   const float* cost;
@@ -67,110 +78,88 @@ __device__ __forceinline__ float norm_log(float sum) {
   return y;
 }
 
-// Per-warp shared memory carve-up (all offsets in floats, 16-byte aligned).
-struct WarpSmem {
-  float* ring;      // ns * (3*lrow + lmat)
-  uint64_t* bars;   // ns
-  float* hs;        // 32*K : h of the current pixel
-  float* taps;      // 2 * (Lv+1) * 33 : stereo taps + edge weight for 32 pixels
-};
-
+// Shared memory of a block: CPB chains of NW warps each.
+//   per chain: hs   32K floats + kHsPad of +inf on both sides (h of the pixel)
+//              erow 32K floats (exp values, NW > 1 only)
+//              red  16 words   (per-warp partial minima / tie counts / labels)
+//   per warp:  ring ns stages x 3 rows x lroww floats (cost and the two
+//              cross-direction messages of the warp's own labels [+ the
+//              pixel's L x L pairwise matrix, pixel variant]), ns mbarriers,
+//              taps tile 2 x (Lv+1) x 33 floats.
 __host__ __device__ inline int align4(int v) { return (v + 3) & ~3; }
 
 __host__ __device__ inline int stage_floats(int lrow, int lmat) { return 3 * lrow + lmat; }
 
-__host__ __device__ inline int warp_smem_floats(int K, int ns, int lrow, int lmat, int Lv) {
-  const int ring = ns * stage_floats(lrow, lmat);
-  const int bars = 2 * align4(ns);  // ns uint64 -> 2 floats each, padded
-  const int hs = 32 * K;
-  const int taps = align4(2 * (Lv + 1) * 33);
-  return align4(ring) + bars + align4(hs) + taps;
+__host__ __device__ inline int chain_smem_floats(int K) { return align4(32 * K + 2 * kHsPad) + 32 * K + 16; }
+
+__host__ __device__ inline int warp_smem_floats(int ns, int lroww, int lmat, int Lv) {
+  return align4(ns * stage_floats(lroww, lmat)) + 2 * align4(ns) + align4(2 * (Lv + 1) * 33);
 }
 
-template <int K>
-__device__ __forceinline__ WarpSmem carve(float* base, const FwdArgs& a) {
-  WarpSmem s;
-  s.ring = base;
-  float* p = base + align4(a.ns * stage_floats(a.lrow, a.lmat));
-  s.bars = reinterpret_cast<uint64_t*>(p);
-  p += 2 * align4(a.ns);
-  s.hs = p;
-  p += align4(32 * K);
-  s.taps = p;
-  return s;
-}
-
-// Chain geometry helpers --------------------------------------------------
-struct Chain {
-  int n, dir, fixed;  // fixed = y (horizontal) or x (vertical)
-  int len;            // pixels along the chain
-  int64_t HW;
+struct WarpSmem {
+  float* ring;
+  uint64_t* bars;
+  float* taps;
 };
 
-__device__ __forceinline__ int chain_coord(const Chain& c, int i) {
-  // coordinate along the chain of the sender at step i
-  return (c.dir == RIGHT || c.dir == DOWN) ? i : (c.len - 1 - i);
-}
+struct ChainSmem {
+  float* hs;
+  float* erow;
+  float* red;
+};
 
-__device__ __forceinline__ int64_t pix_index(const FwdArgs& a, const Chain& c, int i) {
-  const int v = chain_coord(c, i);
-  const int y = (a.phase == 0) ? c.fixed : v;
-  const int x = (a.phase == 0) ? v : c.fixed;
-  return (static_cast<int64_t>(c.n) * a.H + y) * a.W + x;
-}
+// One scanline of one sweep.  Pixels are addressed by their index within the
+// image (pin = y*W + x); the sender of step i is pin0 + i*dpin and its
+// receiver is one dpin further.
+struct Chain {
+  int n, dir;
+  int pin0, dpin;
+  const float* cost;   // batch item n
+  const float* slot_a; // cross-direction message slots read at the sender
+  const float* slot_b;
+  float* slot_out;     // slot written at the receiver (= the incoming chain slot)
+  int64_t out_off;     // element offset of slot_out within the messages tensor
+  const float* pjump;  // per-pixel pairwise matrices of this direction (pixel variant)
+  int t0, cnt;         // first label of this warp and how many of its labels are < L
+};
 
-// messages offset (floats) of slot `slot` at pixel linear index p of batch n
-__device__ __forceinline__ int64_t msg_off(const FwdArgs& a, int n, int slot, int64_t p) {
-  const int64_t HW = static_cast<int64_t>(a.H) * a.W;
-  const int64_t pin = p - static_cast<int64_t>(n) * HW;  // pixel index within image
-  return ((static_cast<int64_t>(n) * 4 + slot) * HW + pin) * a.L;
-}
-
-// Issues the ring stage for step i (cost + the two cross-direction messages
-// [+ the per-pixel pairwise matrix]).
+// Issues the ring stage for step i: the warp's labels [t0, t0+cnt) of the
+// sender's cost and cross-direction messages.
 template <int VARIANT>
-__device__ __forceinline__ void issue_stage(const FwdArgs& a, const Chain& c, const WarpSmem& sm,
-                                            int i, int lane) {
-  const int st = i % a.ns;
-  float* dst = sm.ring + static_cast<int64_t>(st) * stage_floats(a.lrow, a.lmat);
-  const int64_t p = pix_index(a, c, i);
-  const int sa = (a.phase == 0) ? UP : RIGHT;
-  const int sb = (a.phase == 0) ? DOWN : LEFT;
-  const float* src0 = a.cost + p * a.L;
-  const float* src1 = a.msgs + msg_off(a, c.n, sa, p);
-  const float* src2 = a.msgs + msg_off(a, c.n, sb, p);
-  const float* src3 = nullptr;
-  int bytes3 = 0;
-  if (VARIANT == BPL_LBP_SEM_PIXEL) {
-    const int v = chain_coord(c, i);
-    const int y = (a.phase == 0) ? c.fixed : v;
-    const int x = (a.phase == 0) ? v : c.fixed;
-    src3 = a.jump + (((static_cast<int64_t>(c.dir) * a.H + y) * a.W + x) * a.L) * a.L;
-    bytes3 = a.L * a.L * 4;
-  }
+__device__ __forceinline__ void issue_stage(const FwdArgs& a, const Chain& c, const WarpSmem& sm, int lroww,
+                                            int i, int st, int lane) {
+  float* dst = sm.ring + st * stage_floats(lroww, a.lmat);
+  const int64_t po = static_cast<int64_t>(c.pin0 + i * c.dpin) * a.L + c.t0;
+  const float* src0 = c.cost + po;
+  const float* src1 = c.slot_a + po;
+  const float* src2 = c.slot_b + po;
+  const float* src3 = (VARIANT == BPL_LBP_SEM_PIXEL) ? c.pjump + (po - c.t0) * a.L : nullptr;
   if (a.vec4) {
     if (lane == 0) {
-      const uint32_t rb = static_cast<uint32_t>(a.L) * 4u;
+      const uint32_t rb = static_cast<uint32_t>(c.cnt) * 4u;
+      const uint32_t mb = (VARIANT == BPL_LBP_SEM_PIXEL) ? static_cast<uint32_t>(a.L * a.L) * 4u : 0u;
       fence_proxy_async();
-      mbar_arrive_expect_tx(&sm.bars[st], 3u * rb + static_cast<uint32_t>(bytes3));
-      bulk_g2s(dst, src0, rb, &sm.bars[st]);
-      bulk_g2s(dst + a.lrow, src1, rb, &sm.bars[st]);
-      bulk_g2s(dst + 2 * a.lrow, src2, rb, &sm.bars[st]);
-      if (VARIANT == BPL_LBP_SEM_PIXEL) bulk_g2s(dst + 3 * a.lrow, src3, static_cast<uint32_t>(bytes3), &sm.bars[st]);
+      mbar_arrive_expect_tx(&sm.bars[st], 3u * rb + mb);
+      if (rb > 0) {
+        bulk_g2s(dst, src0, rb, &sm.bars[st]);
+        bulk_g2s(dst + lroww, src1, rb, &sm.bars[st]);
+        bulk_g2s(dst + 2 * lroww, src2, rb, &sm.bars[st]);
+      }
+      if (VARIANT == BPL_LBP_SEM_PIXEL) bulk_g2s(dst + 3 * lroww, src3, mb, &sm.bars[st]);
     }
   } else {
-    for (int t = lane; t < a.L; t += 32) {
+    for (int t = lane; t < c.cnt; t += 32) {
       cp_async4(dst + t, src0 + t);
-      cp_async4(dst + a.lrow + t, src1 + t);
-      cp_async4(dst + 2 * a.lrow + t, src2 + t);
+      cp_async4(dst + lroww + t, src1 + t);
+      cp_async4(dst + 2 * lroww + t, src2 + t);
     }
     if (VARIANT == BPL_LBP_SEM_PIXEL)
-      for (int t = lane; t < a.L * a.L; t += 32) cp_async4(dst + 3 * a.lrow + t, src3 + t);
+      for (int t = lane; t < a.L * a.L; t += 32) cp_async4(dst + 3 * lroww + t, src3 + t);
   }
 }
 
-// Stereo taps + edge weight for the 32 pixels of block b: lane j loads pixel
-// (32b + j).  Held in registers until written to the tile.
+// Stereo taps + edge weight for the 32 pixels of block b: lane j loads the
+// sender of step 32b + j.  Held in registers until written to the tile.
 struct TapRegs {
   float t[16];
   float w;
@@ -180,15 +169,13 @@ __device__ __forceinline__ void load_taps(const FwdArgs& a, const Chain& c, int 
                                           TapRegs& r, bool stereo) {
   const int i = 32 * b + lane;
   if (i >= nsteps) return;
-  const int v = chain_coord(c, i);
-  const int y = (a.phase == 0) ? c.fixed : v;
-  const int x = (a.phase == 0) ? v : c.fixed;
   const int64_t HW = static_cast<int64_t>(a.H) * a.W;
+  const int pin = c.pin0 + i * c.dpin;
   const int ne = (a.eb == 1) ? 0 : c.n;
-  r.w = __ldg(a.edge + (static_cast<int64_t>(ne) * 4 + c.dir) * HW + static_cast<int64_t>(y) * a.W + x);
+  r.w = __ldg(a.edge + (static_cast<int64_t>(ne) * 4 + c.dir) * HW + pin);
   if (stereo) {
     const int nj = (a.jb == 1) ? 0 : c.n;
-    const float* base = a.jump + ((static_cast<int64_t>(nj) * 4 + c.dir) * a.Lv) * HW + static_cast<int64_t>(y) * a.W + x;
+    const float* base = a.jump + ((static_cast<int64_t>(nj) * 4 + c.dir) * a.Lv) * HW + pin;
 #pragma unroll
     for (int k = 0; k < 16; ++k)
       if (k < a.Lv) r.t[k] = __ldg(base + static_cast<int64_t>(k) * HW);
@@ -206,41 +193,113 @@ __device__ __forceinline__ void store_taps(const FwdArgs& a, float* tile, int la
   }
 }
 
-template <int K, int VARIANT>
+// Barrier over the NW warps of one chain (named barrier `id`), returning the
+// AND of `v` over them.
+template <int NW>
+__device__ __forceinline__ bool chain_sync_and(int id, bool v) {
+  if (NW == 1) return __all_sync(FULL, v);
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n barrier.red.and.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(r)
+      : "r"(static_cast<uint32_t>(v)), "r"(id), "r"(NW * 32)
+      : "memory");
+  return r != 0;
+}
+
+template <int NW>
+__device__ __forceinline__ void chain_sync(int id) {
+  if (NW == 1) {
+    __syncwarp();
+    return;
+  }
+  asm volatile("barrier.sync.aligned %0, %1;" ::"r"(id), "r"(NW * 32) : "memory");
+}
+
+// K labels per lane over the chain (label = lane + 32k), KW = K/NW of them
+// owned by each of the chain's NW warps (slots [w*KW, (w+1)*KW)).
+template <int K, int VARIANT, int NW>
 __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
+  static_assert(K % NW == 0, "labels must split evenly over the chain's warps");
+  static_assert(NW == 1 || VARIANT != BPL_LBP_SEM_PIXEL, "pixel variant runs one warp per chain");
+  constexpr int KW = K / NW;
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const int chain_id = blockIdx.x * (blockDim.x >> 5) + wib;
-  if (chain_id >= a.nchains) return;  // whole warp leaves; no block barriers below
+  const int cpb = (blockDim.x >> 5) / NW;  // chains per block
+  const int cic = wib / NW;                // chain within block
+  const int wic = wib % NW;                // warp within chain
+  const int chain_id = blockIdx.x * cpb + cic;
+  if (chain_id >= a.nchains) return;  // the chain's warps leave together; no block-wide barriers below
+  const int bar_id = 1 + cic;
 
-  const int per_warp = warp_smem_floats(K, a.ns, a.lrow, a.lmat, a.Lv);
-  WarpSmem sm = carve<K>(smem + static_cast<int64_t>(wib) * per_warp, a);
+  const int L = a.L;
+  const int lroww = 32 * KW;
+  ChainSmem cs;
+  {
+    float* p = smem + cic * chain_smem_floats(K);
+    cs.hs = p + kHsPad;
+    cs.erow = p + align4(32 * K + 2 * kHsPad);
+    cs.red = cs.erow + 32 * K;
+  }
+  WarpSmem sm;
+  {
+    float* p = smem + cpb * chain_smem_floats(K) + wib * warp_smem_floats(a.ns, lroww, a.lmat, a.Lv);
+    sm.ring = p;
+    p += align4(a.ns * stage_floats(lroww, a.lmat));
+    sm.bars = reinterpret_cast<uint64_t*>(p);
+    p += 2 * align4(a.ns);
+    sm.taps = p;
+  }
   // exp table for lane-varying lookups: every warp writes the same values
   __shared__ float s_ehi[64], s_elo[64];
   s_ehi[lane] = crm::kTab.exp_hi[lane];
   s_ehi[lane + 32] = crm::kTab.exp_hi[lane + 32];
   s_elo[lane] = crm::kTab.exp_lo[lane];
   s_elo[lane + 32] = crm::kTab.exp_lo[lane + 32];
+  if (wic == 0 && lane < kHsPad) {
+    cs.hs[-1 - lane] = __int_as_float(0x7f800000);
+    cs.hs[32 * K + lane] = __int_as_float(0x7f800000);
+  }
   __syncwarp();
 
+  const int64_t HW = static_cast<int64_t>(a.H) * a.W;
+  const int64_t HWL = HW * L;
   Chain c;
-  const int r = chain_id >> 1;
-  if (a.phase == 0) {
-    c.dir = (chain_id & 1) ? LEFT : RIGHT;
-    c.n = r / a.H;
-    c.fixed = r % a.H;
-    c.len = a.W;
-  } else {
-    c.dir = (chain_id & 1) ? UP : DOWN;
-    c.n = r / a.W;
-    c.fixed = r % a.W;
-    c.len = a.H;
+  int len;
+  {
+    const int r = chain_id >> 1;
+    if (a.phase == 0) {
+      c.dir = (chain_id & 1) ? LEFT : RIGHT;
+      c.n = r / a.H;
+      const int y = r % a.H;
+      len = a.W;
+      c.pin0 = y * a.W + ((c.dir == RIGHT) ? 0 : a.W - 1);
+      c.dpin = (c.dir == RIGHT) ? 1 : -1;
+    } else {
+      c.dir = (chain_id & 1) ? UP : DOWN;
+      c.n = r / a.W;
+      const int x = r % a.W;
+      len = a.H;
+      c.pin0 = ((c.dir == DOWN) ? 0 : a.H - 1) * a.W + x;
+      c.dpin = (c.dir == DOWN) ? a.W : -a.W;
+    }
   }
-  const int nsteps = c.len - 1;
+  const int nsteps = len - 1;
   if (nsteps <= 0) return;
   const int od = c.dir ^ 1;
-  const int L = a.L;
+  const int sa = (a.phase == 0) ? UP : RIGHT;
+  const int sb = (a.phase == 0) ? DOWN : LEFT;
+  c.cost = a.cost + static_cast<int64_t>(c.n) * HWL;
+  c.slot_a = a.msgs + (static_cast<int64_t>(c.n) * 4 + sa) * HWL;
+  c.slot_b = a.msgs + (static_cast<int64_t>(c.n) * 4 + sb) * HWL;
+  c.out_off = (static_cast<int64_t>(c.n) * 4 + od) * HWL;
+  c.slot_out = a.msgs + c.out_off;
+  c.pjump = (VARIANT == BPL_LBP_SEM_PIXEL) ? a.jump + static_cast<int64_t>(c.dir) * HWL * L : nullptr;
+  c.t0 = 32 * KW * wic;
+  c.cnt = max(0, min(lroww, L - c.t0));
+  float* scale_out = a.scale + (static_cast<int64_t>(c.n) * 4 + od) * HW;
+  const float* gjump = (VARIANT == BPL_LBP_SEM_GLOBAL) ? a.jump + static_cast<int64_t>(c.dir) * L * L : nullptr;
   const bool stereo = (VARIANT == BPL_LBP_STEREO);
 
   // ring start-up
@@ -250,20 +309,18 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
   }
   __syncwarp();
   for (int i = 0; i < a.ns; ++i) {
-    if (i < nsteps) issue_stage<VARIANT>(a, c, sm, i, lane);
+    if (i < nsteps) issue_stage<VARIANT>(a, c, sm, lroww, i, i, lane);
     if (!a.vec4) cp_async_commit();
   }
 
-  // incoming chain message at the first sender (slot = chain direction's
-  // opposite side, i.e. the slot the sweep itself writes)
-  float chain[K];
+  // incoming chain message at the first sender: the slot the sweep writes
+  float chain[KW];
   {
-    const int64_t p0 = pix_index(a, c, 0);
-    const float* src = a.msgs + msg_off(a, c.n, od, p0);
+    const float* src = c.slot_out + static_cast<int64_t>(c.pin0) * L;
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const int t = lane + 32 * k;
-      chain[k] = (t < L) ? src[t] : 0.0f;
+    for (int kk = 0; kk < KW; ++kk) {
+      const int t = c.t0 + lane + 32 * kk;
+      chain[kk] = (t < L) ? src[t] : 0.0f;
     }
   }
 
@@ -273,184 +330,336 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
   if (nsteps > 32) load_taps(a, c, 1, lane, nsteps, tr, stereo);
   __syncwarp();
 
+  const int delta = a.delta;
+  const int tile_stride = (a.Lv + 1) * 33;
+  const int sf = stage_floats(lroww, a.lmat);
+  const float kInf = __int_as_float(0x7f800000);
   bool failed = false;
-  for (int i = 0; i < nsteps; ++i) {
-    const int st = i % a.ns;
+  int st = 0;
+  uint32_t par = 0;
+  int pin = c.pin0;
+  for (int i = 0; i < nsteps; ++i, pin += c.dpin) {
     const int j = i & 31;
     const int b = i >> 5;
-    const float* tile = sm.taps + (b & 1) * ((a.Lv + 1) * 33);
-    const float* stg = sm.ring + static_cast<int64_t>(st) * stage_floats(a.lrow, a.lmat);
+    const float* tile = sm.taps + (b & 1) * tile_stride;
+    const float* stg = sm.ring + st * sf;
 
-    // wait for stage i
+    // wait for stage i (own labels)
+    bool ok = true;
     if (a.vec4) {
-      const bool ok = mbar_wait_bounded(&sm.bars[st], static_cast<uint32_t>((i / a.ns) & 1));
-      if (!__all_sync(FULL, ok)) { failed = true; break; }
+      ok = mbar_wait_bounded(&sm.bars[st], par);
     } else {
       cp_async_wait<kRingCpAsync - 1>();  // groups 0..i have landed
-      __syncwarp();
     }
+    __syncwarp();
 
     // h = cost + incoming messages except the chain direction's own slot,
     // added in the reference order RIGHT, LEFT, UP, DOWN.
-    float h[K];
+    float h[KW];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const int t = lane + 32 * k;
-      if (t < L) {
-        const float cst = stg[t];
-        const float va = stg[a.lrow + t];
-        const float vb = stg[2 * a.lrow + t];
-        h[k] = (a.phase == 0) ? __fadd_rn(__fadd_rn(__fadd_rn(cst, chain[k]), va), vb)
-                              : __fadd_rn(__fadd_rn(__fadd_rn(cst, va), vb), chain[k]);
+    for (int kk = 0; kk < KW; ++kk) {
+      const int tl = lane + 32 * kk;  // label within the warp's range
+      if (c.t0 + tl < L) {
+        const float cst = stg[tl];
+        const float va = stg[lroww + tl];
+        const float vb = stg[2 * lroww + tl];
+        h[kk] = (a.phase == 0) ? __fadd_rn(__fadd_rn(__fadd_rn(cst, chain[kk]), va), vb)
+                               : __fadd_rn(__fadd_rn(__fadd_rn(cst, va), vb), chain[kk]);
       } else {
-        h[k] = 0.0f;
+        h[kk] = kInf;  // never a minimum
       }
+      cs.hs[c.t0 + tl] = h[kk];
     }
-    float pw_reg[K];  // per-pixel pairwise row read later (pixel variant)
-    (void)pw_reg;
+    // partial minimum over the warp's labels, with its tie count and label
+    float pm = h[0];
 #pragma unroll
-    for (int k = 0; k < K; ++k) sm.hs[lane + 32 * k] = h[k];
-
-    // pixel variant: keep the stage until the window loop has read it
+    for (int kk = 1; kk < KW; ++kk) pm = fminf(pm, h[kk]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pm = fminf(pm, __shfl_xor_sync(FULL, pm, o));
+    int pcnt = 0, plab = 0;
+#pragma unroll
+    for (int kk = 0; kk < KW; ++kk) {
+      const unsigned m = __ballot_sync(FULL, h[kk] == pm);
+      pcnt += __popc(m);
+      if (m) plab = c.t0 + 32 * kk + __ffs(m) - 1;
+    }
+    if (NW > 1 && lane == 0) {
+      cs.red[wic] = pm;
+      reinterpret_cast<int*>(cs.red)[4 + wic] = pcnt;
+      reinterpret_cast<int*>(cs.red)[8 + wic] = plab;
+    }
     __syncwarp();
     if (VARIANT != BPL_LBP_SEM_PIXEL) {
-      // stage st is free: refill it with step i + ns
-      if (i + a.ns < nsteps) issue_stage<VARIANT>(a, c, sm, i + a.ns, lane);
+      // stage consumed: refill it with step i + ns
+      if (i + a.ns < nsteps) issue_stage<VARIANT>(a, c, sm, lroww, i + a.ns, st, lane);
       if (!a.vec4) cp_async_commit();
     }
+    // h of the whole pixel and the partial minima are visible to the chain
+    if (!chain_sync_and<NW>(bar_id, ok)) {
+      failed = true;
+      break;
+    }
 
-    // per-pixel parameters
     const float w = tile[a.Lv * 33 + j];
-    const int delta = a.delta;
-    float msg[K];
-    int am[K];
+    float msg[KW];
+    int am[KW];
+    float e[KW];
 
     if (delta >= L) {
       // full minimisation (lbp_min_sum_kernel.cu:88-111): last minimiser wins
 #pragma unroll
-      for (int k = 0; k < K; ++k) {
-        const int t = lane + 32 * k;
+      for (int kk = 0; kk < KW; ++kk) {
+        const int t = c.t0 + lane + 32 * kk;
         float m = 1e15f;
         int arg = 0;
         if (t < L) {
           for (int s = 0; s < L; ++s) {
             float f;
             if (stereo) {
-              int ti = a.Lv / 2 + (t - s);
-              ti = max(1, min(a.Lv - 1, ti));
+              const int ti = max(1, min(a.Lv - 1, a.Lv / 2 + (t - s)));
               f = tile[ti * 33 + j];
             } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
-              f = __ldg(a.jump + (static_cast<int64_t>(c.dir) * L + s) * L + t);
+              f = __ldg(gjump + s * L + t);
             } else {
-              f = stg[3 * a.lrow + s * L + t];
+              f = stg[3 * lroww + s * L + t];
             }
-            const float nm = __fmaf_rn(f, w, sm.hs[s]);
+            const float nm = __fmaf_rn(f, w, cs.hs[s]);
             m = fminf(m, nm);
             if (m == nm) arg = s;
           }
         }
-        msg[k] = m;
-        am[k] = arg;
+        msg[kk] = m;
+        am[kk] = arg;
+      }
+      bool all_ok = true;
+      bool eok[KW];
+#pragma unroll
+      for (int kk = 0; kk < KW; ++kk) {
+        eok[kk] = crm::exp_fast(msg[kk], e[kk], s_ehi, s_elo);
+        if (c.t0 + lane + 32 * kk >= L) {
+          e[kk] = 0.0f;
+          eok[kk] = true;
+        }
+        all_ok = all_ok && eok[kk];
+      }
+      if (!__all_sync(FULL, all_ok)) {
+#pragma unroll
+        for (int kk = 0; kk < KW; ++kk)
+          if (!eok[kk]) e[kk] = static_cast<float>(exp(static_cast<double>(msg[kk])));
       }
     } else {
-      // truncated branch (lbp_min_sum_kernel.cu:112-164)
-      float tv[K];
-      int tl[K];
-#pragma unroll
-      for (int k = 0; k < K; ++k) {
-        tv[k] = h[k];
-        tl[k] = lane + 32 * k;
-      }
-      float min_h;
-      int argmin_h;
-      tree_argmin<K>(tv, tl, L, lane, min_h, argmin_h);
+      // Truncated branch (lbp_min_sum_kernel.cu:112-164).  The reference
+      // starts from the global candidate fmaf(L2, w, min h) and scans the
+      // window in increasing label order with `<=`; that equals taking the
+      // window's own minimum (last label on ties) when it is <= the global
+      // candidate, so the window scan needs no global minimum and runs first.
       float L2, off = 0.0f;
       if (stereo) {
         L2 = tile[(a.Lv - 1) * 33 + j];
         off = tile[0 * 33 + j];
       } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
-        L2 = __ldg(a.jump + (static_cast<int64_t>(c.dir) * L + 0) * L + (L - 1));
+        L2 = __ldg(gjump + (L - 1));
       } else {
-        L2 = stg[3 * a.lrow + (L - 1)];
+        L2 = stg[3 * lroww + (L - 1)];
       }
+      float wv[KW];
+      int wa[KW];
+      if (stereo && delta <= kFastDelta && off == 0.0f) {
+        // Zero offset: the window is [t-delta, t+delta] clipped to [0, L),
+        // and the tap of sender s = t + jd is clamp(Lv/2 - jd, 1, Lv-1), the
+        // same for every label.  hs holds +inf outside [0, L), which never
+        // wins against the finite global candidate, in place of the clipping.
+        float fj[2 * kFastDelta + 1];
 #pragma unroll
-      for (int k = 0; k < K; ++k) {
-        const int t = lane + 32 * k;
-        float m = __fmaf_rn(L2, w, min_h);
-        int arg = argmin_h;
-        if (t < L) {
-          int start, stop;
-          if (stereo) {
-            start = sat_u16(roundf(__fsub_rn(__fadd_rn(static_cast<float>(t - (delta - 1)), off), 1.0f)));
-            stop = min(sat_u16(roundf(__fadd_rn(__fadd_rn(static_cast<float>(t + delta), off), 1.0f))), L);
-          } else {
-            start = max(t - delta + 1, 0);
-            stop = min(t + delta - 1, L - 1) + 1;
+        for (int q = 0; q <= 2 * kFastDelta; ++q) {
+          const int ti = max(1, min(a.Lv - 1, a.Lv / 2 - (q - kFastDelta)));
+          fj[q] = tile[ti * 33 + j];
+        }
+        if (delta == 3) {
+#pragma unroll
+          for (int kk = 0; kk < KW; ++kk) {
+            const int t = c.t0 + lane + 32 * kk;
+            float m = kInf;
+            int arg = 0;
+#pragma unroll
+            for (int q = kFastDelta - 3; q <= kFastDelta + 3; ++q) {
+              const float nm = __fmaf_rn(fj[q], w, cs.hs[t + q - kFastDelta]);
+              const bool take = nm <= m;
+              m = take ? nm : m;
+              arg = take ? t + q - kFastDelta : arg;
+            }
+            wv[kk] = m;
+            wa[kk] = arg;
           }
-          for (int s = start; s < stop; ++s) {
-            float f;
-            if (stereo) {
-              int ti = a.Lv / 2 + (t - s);
-              ti = max(1, min(a.Lv - 1, ti));
-              f = tile[ti * 33 + j];
-            } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
-              f = __ldg(a.jump + (static_cast<int64_t>(c.dir) * L + s) * L + t);
-            } else {
-              f = stg[3 * a.lrow + s * L + t];
+        } else {
+#pragma unroll
+          for (int kk = 0; kk < KW; ++kk) {
+            const int t = c.t0 + lane + 32 * kk;
+            float m = kInf;
+            int arg = 0;
+#pragma unroll
+            for (int q = 0; q <= 2 * kFastDelta; ++q) {
+              const int jd = q - kFastDelta;
+              const float nm = __fmaf_rn(fj[q], w, cs.hs[t + jd]);
+              const bool take = (jd >= -delta) && (jd <= delta) && (nm <= m);  // branch-free
+              m = take ? nm : m;
+              arg = take ? t + jd : arg;
             }
-            const float nm = __fmaf_rn(f, w, sm.hs[s]);
-            if (nm <= m) {
-              m = nm;
-              arg = s;
-            }
+            wv[kk] = m;
+            wa[kk] = arg;
           }
         }
-        msg[k] = m;
-        am[k] = arg;
+      } else {
+#pragma unroll
+        for (int kk = 0; kk < KW; ++kk) {
+          const int t = c.t0 + lane + 32 * kk;
+          float m = kInf;
+          int arg = 0;
+          if (t < L) {
+            int start, stop;
+            if (stereo) {
+              start = sat_u16(roundf(__fsub_rn(__fadd_rn(static_cast<float>(t - (delta - 1)), off), 1.0f)));
+              stop = min(sat_u16(roundf(__fadd_rn(__fadd_rn(static_cast<float>(t + delta), off), 1.0f))), L);
+            } else {
+              start = max(t - delta + 1, 0);
+              stop = min(t + delta - 1, L - 1) + 1;
+            }
+            for (int s = start; s < stop; ++s) {
+              float f;
+              if (stereo) {
+                const int ti = max(1, min(a.Lv - 1, a.Lv / 2 + (t - s)));
+                f = tile[ti * 33 + j];
+              } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
+                f = __ldg(gjump + s * L + t);
+              } else {
+                f = stg[3 * lroww + s * L + t];
+              }
+              const float nm = __fmaf_rn(f, w, cs.hs[s]);
+              if (nm <= m) {
+                m = nm;
+                arg = s;
+              }
+            }
+          }
+          wv[kk] = m;
+          wa[kk] = arg;
+        }
+      }
+      // The global candidate needs only the minimum value of h, which any
+      // reduction order gives exactly; its exp is shared by every label the
+      // window does not win (most of them).
+      float min_h = pm;
+      int argmin_h = plab, tot = pcnt;
+      if (NW > 1) {
+        min_h = cs.red[0];
+#pragma unroll
+        for (int w2 = 1; w2 < NW; ++w2) min_h = fminf(min_h, cs.red[w2]);
+        tot = 0;
+#pragma unroll
+        for (int w2 = 0; w2 < NW; ++w2)
+          if (cs.red[w2] == min_h) {
+            tot += reinterpret_cast<const int*>(cs.red)[4 + w2];
+            argmin_h = reinterpret_cast<const int*>(cs.red)[8 + w2];
+          }
+      }
+      const float msg_g = __fmaf_rn(L2, w, min_h);
+      float e_g;
+      if (!crm::exp_fast(msg_g, e_g, s_ehi, s_elo)) e_g = static_cast<float>(exp(static_cast<double>(msg_g)));
+      // exact ties of the minimum: the reference tree picks the label
+      if (tot > 1) {
+        float tv[K];
+        int tl[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          tv[k] = cs.hs[lane + 32 * k];
+          tl[k] = lane + 32 * k;
+        }
+        float mv;
+        tree_argmin<K>(tv, tl, L, lane, mv, argmin_h);
+      }
+      bool all_ok = true;
+#pragma unroll
+      for (int kk = 0; kk < KW; ++kk) {
+        const bool valid = c.t0 + lane + 32 * kk < L;
+        const bool win = valid && wv[kk] <= msg_g;
+        msg[kk] = win ? wv[kk] : msg_g;
+        am[kk] = win ? wa[kk] : argmin_h;
+        e[kk] = valid ? e_g : 0.0f;
+        const bool own = win && wv[kk] != msg_g;
+        if (__any_sync(FULL, own)) {
+          // slot with window winners: their own exp (straight-line code)
+          float ex;
+          const bool okx = crm::exp_fast(wv[kk], ex, s_ehi, s_elo);
+          e[kk] = own ? ex : e[kk];
+          all_ok = all_ok && (okx || !own);
+        }
+      }
+      if (!__all_sync(FULL, all_ok)) {
+        // rounding undecided in float-float (rare): the reference expression
+#pragma unroll
+        for (int kk = 0; kk < KW; ++kk) {
+          const bool valid = c.t0 + lane + 32 * kk < L;
+          if (valid && msg[kk] != msg_g) e[kk] = static_cast<float>(exp(static_cast<double>(msg[kk])));
+        }
       }
     }
 
     if (VARIANT == BPL_LBP_SEM_PIXEL) {
       __syncwarp();
-      if (i + a.ns < nsteps) issue_stage<VARIANT>(a, c, sm, i + a.ns, lane);
+      if (i + a.ns < nsteps) issue_stage<VARIANT>(a, c, sm, lroww, i + a.ns, st, lane);
       if (!a.vec4) cp_async_commit();
     }
 
-    // normalisation (lbp_min_sum_kernel.cu:166-181)
-    float e[K];
+    // normalisation (lbp_min_sum_kernel.cu:166-181): sum tree over all labels
+    float sum;
+    if (NW == 1) {
+      float ev[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) e[k] = (lane + 32 * k < L) ? norm_exp(msg[k], s_ehi, s_elo) : 0.0f;
-    const float sum = tree_sum<K>(e, L, lane);
-    const double sum_exp = fmax(static_cast<double>(sum), 1e-45);
+      for (int k = 0; k < K; ++k) ev[k] = e[k % KW];
+      sum = tree_sum<K>(ev, L, lane);
+    } else {
+#pragma unroll
+      for (int kk = 0; kk < KW; ++kk) cs.erow[c.t0 + lane + 32 * kk] = e[kk];
+      chain_sync<NW>(bar_id);
+      float ev[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) ev[k] = cs.erow[lane + 32 * k];
+      sum = tree_sum<K>(ev, L, lane);
+    }
     const float lse = norm_log(sum);
 
     // write the message at the receiver
-    const int64_t pq = pix_index(a, c, i) + ((a.phase == 0) ? ((c.dir == RIGHT) ? 1 : -1)
-                                                            : ((c.dir == DOWN) ? a.W : -a.W));
-    const int64_t qo = msg_off(a, c.n, od, pq);
-    float* dstm = a.msgs + qo;
+    const int pq = pin + c.dpin;
+    const int64_t qo = static_cast<int64_t>(pq) * L;
+    float* dstm = c.slot_out + qo;
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const int t = lane + 32 * k;
-      const float o = __fsub_rn(msg[k], lse);
-      chain[k] = o;
+    for (int kk = 0; kk < KW; ++kk) {
+      const int t = c.t0 + lane + 32 * kk;
+      const float o = __fsub_rn(msg[kk], lse);
+      chain[kk] = o;
       if (t < L) {
         dstm[t] = o;
-        if (a.argmin_kind == BPL_ARGMIN_F32) static_cast<float*>(a.argmin)[qo + t] = static_cast<float>(am[k]);
-        else if (a.argmin_kind == BPL_ARGMIN_U8) static_cast<uint8_t*>(a.argmin)[qo + t] = static_cast<uint8_t>(am[k]);
-        else if (a.argmin_kind == BPL_ARGMIN_U16) static_cast<uint16_t*>(a.argmin)[qo + t] = static_cast<uint16_t>(am[k]);
+        const int64_t ao = c.out_off + qo + t;
+        if (a.argmin_kind == BPL_ARGMIN_U8) static_cast<uint8_t*>(a.argmin)[ao] = static_cast<uint8_t>(am[kk]);
+        else if (a.argmin_kind == BPL_ARGMIN_F32) static_cast<float*>(a.argmin)[ao] = static_cast<float>(am[kk]);
+        else if (a.argmin_kind == BPL_ARGMIN_U16) static_cast<uint16_t*>(a.argmin)[ao] = static_cast<uint16_t>(am[kk]);
       }
     }
-    if (lane == 0) a.scale[qo / L] = static_cast<float>(sum_exp);
+    // (float)max((double)sum, 1e-45): the smallest positive float when sum is 0
+    if (wic == 0 && lane == 0) scale_out[pq] = (sum > 0.0f) ? sum : __int_as_float(1);
 
     // next tap block
     if (j == 31 || i == nsteps - 1) {
       __syncwarp();
       if (32 * (b + 1) < nsteps) {
-        store_taps(a, sm.taps + ((b + 1) & 1) * ((a.Lv + 1) * 33), lane, tr, stereo);
+        store_taps(a, sm.taps + ((b + 1) & 1) * tile_stride, lane, tr, stereo);
         if (32 * (b + 2) < nsteps) load_taps(a, c, b + 2, lane, nsteps, tr, stereo);
       }
       __syncwarp();
+    }
+    if (++st == a.ns) {
+      st = 0;
+      par ^= 1u;
     }
   }
 
@@ -463,27 +672,46 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
   }
   if (!a.vec4) cp_async_wait<0>();
 }
-// Host-side launch of both phases for one (K, variant) instantiation.
-template <int K, int V>
-int launch_k(const FwdArgs& a0, cudaStream_t stream) {
-  FwdArgs a = a0;
-  const int per_warp = warp_smem_floats(K, a.ns, a.lrow, a.lmat, a.Lv) * 4;
-  // up to 4 warps (scanlines) per block while the block fits in 200 KB
-  const int kWarpsPerBlock = std::max(1, std::min(4, (200 * 1024) / per_warp));
-  const size_t smem = static_cast<size_t>(per_warp) * kWarpsPerBlock;
-  auto kern = lbp_forward_kernel<K, V>;
+
+// Host-side launch of one phase for one (K, variant, NW) instantiation.
+template <int K, int V, int NW>
+int launch_phase(const FwdArgs& a, cudaStream_t stream) {
+  const int lroww = 32 * (K / NW);
+  const size_t per_chain = 4 * (static_cast<size_t>(chain_smem_floats(K)) +
+                                static_cast<size_t>(NW) * warp_smem_floats(a.ns, lroww, a.lmat, a.Lv));
+  // chains per block: up to 4 warps while the block fits in 200 KB
+  const int cpb = std::max(1, std::min(4 / NW, static_cast<int>((200 * 1024) / per_chain)));
+  const size_t smem = per_chain * cpb;
+  auto kern = lbp_forward_kernel<K, V, NW>;
   if (smem > 48 * 1024) {
     if (static_cast<int>(smem) > max_smem_optin())
       return set_error(BPL_ERR_UNSUPPORTED, "lbp_forward: shared memory %zu exceeds device limit", smem);
     BPL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
                  "cudaFuncSetAttribute");
   }
+  const int blocks = (a.nchains + cpb - 1) / cpb;
+  kern<<<blocks, 32 * NW * cpb, smem, stream>>>(a);
+  BPL_CUDA_TRY(cudaGetLastError(), "lbp_forward launch");
+  return BPL_OK;
+}
+
+// Scanlines of a phase that a one-warp-per-scanline launch keeps busy: below
+// about six per SM the sweep is latency-bound and the labels of each scanline
+// are split over several warps.
+inline bool split_chains(int nchains) { return nchains < kSplitChainsPerSm * sm_count(); }
+
+// K: register slots per lane (K * 32 >= L).  KS, NS: the instantiation and
+// warp count used when a phase's scanlines are split.
+template <int K, int V, int KS, int NS>
+int launch_k(const FwdArgs& a0, cudaStream_t stream) {
+  FwdArgs a = a0;
   for (int phase = 0; phase < 2; ++phase) {
     a.phase = phase;
     a.nchains = 2 * a.B * (phase == 0 ? a.H : a.W);
-    const int blocks = (a.nchains + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    kern<<<blocks, 32 * kWarpsPerBlock, smem, stream>>>(a);
-    BPL_CUDA_TRY(cudaGetLastError(), "lbp_forward launch");
+    int st;
+    if (NS > 1 && split_chains(a.nchains)) st = launch_phase<KS, V, NS>(a, stream);
+    else st = launch_phase<K, V, 1>(a, stream);
+    if (st != BPL_OK) return st;
   }
   return BPL_OK;
 }
@@ -491,29 +719,44 @@ int launch_k(const FwdArgs& a0, cudaStream_t stream) {
 template <int V>
 int dispatch_k(const FwdArgs& a, cudaStream_t s) {
   const int k = (a.L + 31) / 32;
-  if constexpr (V == BPL_LBP_SEM_PIXEL) {
-    // per-pixel L x L matrices: L <= 96 (checked at the entry point)
-    if (k == 1) return launch_k<1, V>(a, s);
-    if (k == 2) return launch_k<2, V>(a, s);
-    return launch_k<3, V>(a, s);
-  }
-  switch (k) {
-    case 1: return launch_k<1, V>(a, s);
-    case 2: return launch_k<2, V>(a, s);
-    case 3: return launch_k<3, V>(a, s);
-    case 4: return launch_k<4, V>(a, s);
-    case 5: return launch_k<5, V>(a, s);
-    case 6: return launch_k<6, V>(a, s);
-    case 7: return launch_k<7, V>(a, s);
-    case 8: return launch_k<8, V>(a, s);
-    default:
-      if (k <= 12) return launch_k<12, V>(a, s);
-      if (k <= 16) return launch_k<16, V>(a, s);
-      if (k <= 24) return launch_k<24, V>(a, s);
-      return launch_k<32, V>(a, s);
+  if constexpr (V != BPL_LBP_STEREO) {
+    // semantic variants: one warp per scanline
+    if constexpr (V == BPL_LBP_SEM_PIXEL) {
+      // per-pixel L x L matrices: L <= 96 (checked at the entry point)
+      if (k == 1) return launch_k<1, V, 1, 1>(a, s);
+      if (k == 2) return launch_k<2, V, 2, 1>(a, s);
+      return launch_k<3, V, 3, 1>(a, s);
+    }
+    switch (k) {
+      case 1: return launch_k<1, V, 1, 1>(a, s);
+      case 2: return launch_k<2, V, 2, 1>(a, s);
+      case 3: return launch_k<3, V, 3, 1>(a, s);
+      case 4: return launch_k<4, V, 4, 1>(a, s);
+      default:
+        if (k <= 8) return launch_k<8, V, 8, 1>(a, s);
+        if (k <= 16) return launch_k<16, V, 16, 1>(a, s);
+        return launch_k<32, V, 32, 1>(a, s);
+    }
+  } else {
+    // (the split-scanline instantiations KS/NS are enabled together with
+    // kSplitChainsPerSm; with it at 0 every phase runs one warp per scanline)
+    switch (k) {
+      case 1: return launch_k<1, V, 1, 1>(a, s);
+      case 2: return launch_k<2, V, 2, 1>(a, s);
+      case 3: return launch_k<3, V, 3, 1>(a, s);
+      case 4: return launch_k<4, V, 4, 1>(a, s);
+      case 5: return launch_k<5, V, 5, 1>(a, s);
+      case 6: return launch_k<6, V, 6, 1>(a, s);
+      case 7: return launch_k<7, V, 7, 1>(a, s);
+      case 8: return launch_k<8, V, 8, 1>(a, s);
+      default:
+        if (k <= 12) return launch_k<12, V, 12, 1>(a, s);
+        if (k <= 16) return launch_k<16, V, 16, 1>(a, s);
+        if (k <= 24) return launch_k<24, V, 24, 1>(a, s);
+        return launch_k<32, V, 32, 1>(a, s);
+    }
   }
 }
-
 
 int lbp_forward_stereo(const FwdArgs& a, cudaStream_t s);
 int lbp_forward_sem_global(const FwdArgs& a, cudaStream_t s);

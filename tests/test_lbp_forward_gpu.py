@@ -68,6 +68,10 @@ STEREO_CASES = [
     ("l256_wide", 11, 1, 3, 70, 256, "scalar", 3, 1, None, 1, 1),
     ("l300_k12", 12, 1, 4, 9, 300, "scalar", 3, 1, None, 1, 1),
     ("l19_odd", 13, 2, 7, 8, 19, "scalar", 3, 2, None, 1, 2),
+    # enough scanlines per phase for one warp per scanline (the small cases
+    # above split each scanline's labels over several warps)
+    ("l64_many_chains", 14, 8, 64, 72, 64, "taps8_off", 3, 1, None, 8, 8),
+    ("l192_many_chains", 15, 2, 240, 260, 192, "scalar", 3, 1, None, 1, 2),
 ]
 
 
