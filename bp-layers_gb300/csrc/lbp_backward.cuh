@@ -96,36 +96,12 @@ __device__ __forceinline__ Smem carve(float* base, const BwdArgs& a, int variant
   return s;
 }
 
-struct Chain {
-  int n, db, fixed, len;
-};
-
-// sender coordinate along the chain at step k
-__device__ __forceinline__ int sender(const Chain& c, int k) {
-  switch (c.db) {
-    case DOWN: return 1 + k;             // undoes the UP sweep
-    case UP: return c.len - 2 - k;       // undoes DOWN
-    case LEFT: return c.len - 2 - k;     // undoes RIGHT
-    default: return 1 + k;               // RIGHT: undoes LEFT
-  }
-}
-
-__device__ __forceinline__ int recv_delta(int db) {
-  // receiver coordinate - sender coordinate
-  return (db == DOWN || db == RIGHT) ? -1 : 1;
-}
-
-__device__ __forceinline__ int64_t pixel(const BwdArgs& a, const Chain& c, int v) {
-  const int y = (a.phase == 0) ? v : c.fixed;
-  const int x = (a.phase == 0) ? c.fixed : v;
-  return static_cast<int64_t>(y) * a.W + x;  // within image
-}
-
 }  // namespace bwd
 
 // LV: number of stereo jump taps when known at compile time (6 or 8), 16 for
-// any Lv <= 16 given at run time, 0 for the semantic variants.
-template <int K, int VARIANT, int LV>
+// any Lv <= 16 given at run time, 0 for the semantic variants.  CROSS: the
+// horizontal phase (LEFT+RIGHT, with the vertical chains' saved gradients).
+template <int K, int VARIANT, int LV, bool CROSS>
 __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   using namespace bwd;
   extern __shared__ __align__(16) float smem[];
@@ -139,31 +115,53 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
 
   const int L = a.L;
   const int64_t HW = static_cast<int64_t>(a.H) * a.W;
-  Chain c;
-  const int r = chain_id >> 1;
-  if (a.phase == 0) {
-    c.db = (chain_id & 1) ? UP : DOWN;
-    c.n = r / a.W;
-    c.fixed = r % a.W;
-    c.len = a.H;
-  } else {
-    c.db = (chain_id & 1) ? RIGHT : LEFT;
-    c.n = r / a.H;
-    c.fixed = r % a.H;
-    c.len = a.W;
+  const int64_t HWL = HW * L;
+  // chain: sender of step k is pin0 + k*dpin (pixel index within the image),
+  // its receiver is dq further
+  int n, db, pin0, dpin, dq, nsteps;
+  {
+    const int r = chain_id >> 1;
+    if (!CROSS) {
+      db = (chain_id & 1) ? UP : DOWN;
+      n = r / a.W;
+      const int x = r % a.W;
+      nsteps = a.H - 1;
+      pin0 = (db == DOWN) ? a.W + x : (a.H - 2) * a.W + x;  // DOWN: y = 1.., UP: y = H-2..
+      dpin = (db == DOWN) ? a.W : -a.W;
+      dq = -dpin;
+    } else {
+      db = (chain_id & 1) ? RIGHT : LEFT;
+      n = r / a.H;
+      const int y = r % a.H;
+      nsteps = a.W - 1;
+      pin0 = (db == LEFT) ? y * a.W + a.W - 2 : y * a.W + 1;  // LEFT: x = W-2.., RIGHT: x = 1..
+      dpin = (db == LEFT) ? -1 : 1;
+      dq = -dpin;
+    }
   }
-  const int fd = c.db ^ 1;
-  const int nsteps = c.len - 1;
-  const bool cross = (a.phase == 1);
+  const int fd = db ^ 1;
   const bool stereo = (VARIANT == BPL_LBP_STEREO);
-  const int nj = (a.jb == 1) ? 0 : c.n;
-  const int ne = (a.eb == 1) ? 0 : c.n;
+  const int nj = (a.jb == 1) ? 0 : n;
+  const int ne = (a.eb == 1) ? 0 : n;
+  const uint32_t am_size = (a.argmin_kind == BPL_ARGMIN_U8) ? 1u : (a.argmin_kind == BPL_ARGMIN_U16 ? 2u : 4u);
+  const float* msgs_db = a.msgs + (static_cast<int64_t>(n) * 4 + db) * HWL;
+  const float* grad_db = a.in_grad + (static_cast<int64_t>(n) * 4 + db) * HWL;
+  const uint8_t* am_db = static_cast<const uint8_t*>(a.argmin) + (static_cast<int64_t>(n) * 4 + db) * HWL * am_size;
+  const float* saved_up = a.saved + (static_cast<int64_t>(n) * 2 + 0) * HWL;
+  const float* saved_dn = a.saved + (static_cast<int64_t>(n) * 2 + 1) * HWL;
+  float* saved_out = a.saved + (static_cast<int64_t>(n) * 2 + (db == UP ? 0 : 1)) * HWL;
+  float* gcost_n = a.grad_cost + static_cast<int64_t>(n) * HWL;
+  const float* scale_db = a.scale + (static_cast<int64_t>(n) * 4 + db) * HW;
+  const float* edge_fd = a.edge + (static_cast<int64_t>(ne) * 4 + fd) * HW;
+  const float* jump_fd = stereo ? a.jump + (static_cast<int64_t>(nj) * 4 + fd) * a.Lv * HW : nullptr;
+  float* gjump_fd = stereo ? a.grad_jump + (static_cast<int64_t>(nj) * 4 + fd) * a.Lv * HW : nullptr;
+  float* gedge_fd = (VARIANT != BPL_LBP_SEM_PIXEL) ? a.grad_edge + (static_cast<int64_t>(ne) * 4 + fd) * HW : nullptr;
 
   // saved rows never written by a sender are read as zero by the horizontal
   // sweeps: the DOWN chain's row 0 and the UP chain's row H-1
-  if (a.phase == 0) {
-    const int v0 = (c.db == DOWN) ? 0 : (a.H - 1);
-    float* dst = a.saved + ((static_cast<int64_t>(c.n) * 2 + (c.db == UP ? 0 : 1)) * HW + pixel(a, c, v0)) * L;
+  if (!CROSS) {
+    const int x = (chain_id >> 1) % a.W;
+    float* dst = saved_out + (static_cast<int64_t>((db == DOWN) ? 0 : a.H - 1) * a.W + x) * L;
     for (int t = lane; t < L; t += 32) dst[t] = 0.0f;
   }
   if (nsteps <= 0) return;
@@ -173,39 +171,30 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   if (VARIANT == BPL_LBP_SEM_GLOBAL)
     for (int t = lane; t < L * L; t += 32) sm.jacc[t] = 0.0f;
 
-  const int rd = recv_delta(c.db);
-  const uint32_t am_size = (a.argmin_kind == BPL_ARGMIN_U8) ? 1u : (a.argmin_kind == BPL_ARGMIN_U16 ? 2u : 4u);
-  auto issue = [&](int k) {
-    const int st = k % a.ns;
-    float* dst = sm.ring + static_cast<int64_t>(st) * stage_floats(a.lrow);
-    const int64_t q = pixel(a, c, sender(c, k) + rd);
-    const int64_t mo = ((static_cast<int64_t>(c.n) * 4 + c.db) * HW + q) * L;
-    const float* s0 = a.msgs + mo;
-    const float* s1 = a.in_grad + mo;
-    const float* s2 = a.saved + ((static_cast<int64_t>(c.n) * 2 + 0) * HW + q) * L;
-    const float* s3 = a.saved + ((static_cast<int64_t>(c.n) * 2 + 1) * HW + q) * L;
+  auto issue = [&](int k, int st) {
+    float* dst = sm.ring + st * stage_floats(a.lrow);
+    const int64_t qo = static_cast<int64_t>(pin0 + k * dpin + dq) * L;
     if (a.vec4) {
       if (lane == 0) {
         const uint32_t rb = static_cast<uint32_t>(L) * 4u;
         const uint32_t ab = a.am_bulk ? static_cast<uint32_t>(L) * am_size : 0u;
         fence_proxy_async();
-        mbar_arrive_expect_tx(&sm.bars[st], (cross ? 4u : 2u) * rb + ab);
-        bulk_g2s(dst, s0, rb, &sm.bars[st]);
-        bulk_g2s(dst + a.lrow, s1, rb, &sm.bars[st]);
-        if (cross) {
-          bulk_g2s(dst + 2 * a.lrow, s2, rb, &sm.bars[st]);
-          bulk_g2s(dst + 3 * a.lrow, s3, rb, &sm.bars[st]);
+        mbar_arrive_expect_tx(&sm.bars[st], (CROSS ? 4u : 2u) * rb + ab);
+        bulk_g2s(dst, msgs_db + qo, rb, &sm.bars[st]);
+        bulk_g2s(dst + a.lrow, grad_db + qo, rb, &sm.bars[st]);
+        if (CROSS) {
+          bulk_g2s(dst + 2 * a.lrow, saved_up + qo, rb, &sm.bars[st]);
+          bulk_g2s(dst + 3 * a.lrow, saved_dn + qo, rb, &sm.bars[st]);
         }
-        if (a.am_bulk)
-          bulk_g2s(dst + 4 * a.lrow, static_cast<const uint8_t*>(a.argmin) + mo * am_size, ab, &sm.bars[st]);
+        if (a.am_bulk) bulk_g2s(dst + 4 * a.lrow, am_db + qo * am_size, ab, &sm.bars[st]);
       }
     } else {
       for (int t = lane; t < L; t += 32) {
-        cp_async4(dst + t, s0 + t);
-        cp_async4(dst + a.lrow + t, s1 + t);
-        if (cross) {
-          cp_async4(dst + 2 * a.lrow + t, s2 + t);
-          cp_async4(dst + 3 * a.lrow + t, s3 + t);
+        cp_async4(dst + t, msgs_db + qo + t);
+        cp_async4(dst + a.lrow + t, grad_db + qo + t);
+        if (CROSS) {
+          cp_async4(dst + 2 * a.lrow + t, saved_up + qo + t);
+          cp_async4(dst + 3 * a.lrow + t, saved_dn + qo + t);
         }
       }
     }
@@ -216,14 +205,13 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   auto load_tile_regs = [&](int b, float (&rg)[18]) {
     const int k = 32 * b + lane;
     if (k >= nsteps) return;
-    const int64_t p = pixel(a, c, sender(c, k));
-    const int64_t q = pixel(a, c, sender(c, k) + rd);
-    rg[a.Lv] = __ldg(a.edge + (static_cast<int64_t>(ne) * 4 + fd) * HW + p);
-    rg[a.Lv + 1] = __ldg(a.scale + (static_cast<int64_t>(c.n) * 4 + c.db) * HW + q);
+    const int p = pin0 + k * dpin;
+    rg[a.Lv] = __ldg(edge_fd + p);
+    rg[a.Lv + 1] = __ldg(scale_db + p + dq);
     if (stereo) {
 #pragma unroll
       for (int j = 0; j < 16; ++j)
-        if (j < a.Lv) rg[j] = __ldg(a.jump + ((static_cast<int64_t>(nj) * 4 + fd) * a.Lv + j) * HW + p);
+        if (j < a.Lv) rg[j] = __ldg(jump_fd + static_cast<int64_t>(j) * HW + p);
     }
   };
   auto store_tile = [&](float* tile, const float (&rg)[18]) {
@@ -238,7 +226,7 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   }
   __syncwarp();
   for (int k = 0; k < a.ns; ++k) {
-    if (k < nsteps) issue(k);
+    if (k < nsteps) issue(k, k);
     if (!a.vec4) cp_async_commit();
   }
   float rg[18];
@@ -255,21 +243,21 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   float* rowH = sm.rows;
   float* rowU = sm.rows + 32 * K;
   float* rowD = sm.rows + 64 * K;
+  const int sf = stage_floats(a.lrow);
 
   bool failed = false;
-  for (int k = 0; k < nsteps; ++k) {
-    const int st = k % a.ns;
+  int st = 0;
+  uint32_t par = 0;
+  int p = pin0;
+  for (int k = 0; k < nsteps; ++k, p += dpin) {
     const int j = k & 31;
     const int b = k >> 5;
     const float* tile = sm.tile + (b & 1) * (trow * 33);
-    const float* stg = sm.ring + static_cast<int64_t>(st) * stage_floats(a.lrow);
-    const int ys = sender(c, k);
-    const int64_t p = pixel(a, c, ys);
-    const int64_t q = pixel(a, c, ys + rd);
-    const int64_t mo = ((static_cast<int64_t>(c.n) * 4 + c.db) * HW + q) * L;
+    const float* stg = sm.ring + st * sf;
+    const int64_t qo = static_cast<int64_t>(p + dq) * L;
 
     if (a.vec4) {
-      const bool ok = mbar_wait_bounded(&sm.bars[st], static_cast<uint32_t>((k / a.ns) & 1));
+      const bool ok = mbar_wait_bounded(&sm.bars[st], par);
       if (!__all_sync(FULL, ok)) { failed = true; break; }
     } else {
       cp_async_wait<kBwdRingCpAsync - 1>();
@@ -281,30 +269,30 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
     int am[K];
     float sg = 0.0f, sa = 0.0f;
     const void* amrow = a.am_bulk ? static_cast<const void*>(stg + 4 * a.lrow)
-                                  : static_cast<const void*>(static_cast<const uint8_t*>(a.argmin) + mo * am_size);
+                                  : static_cast<const void*>(am_db + qo * am_size);
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const int t = lane + 32 * kk;
-      g[kk] = 0.0f; pr[kk] = 0.0f; sU[kk] = 0.0f; sD[kk] = 0.0f; am[kk] = 0;
-      if (t < L) {
-        g[kk] = stg[a.lrow + t];
-        if (cross) {
-          sU[kk] = stg[2 * a.lrow + t];
-          sD[kk] = stg[3 * a.lrow + t];
-        }
-        // exp(m + log S) / S of the reference (:328-341) is exp(m) for a
-        // normalised message m = m_raw - log S
-        pr[kk] = expf(stg[t]);
-        if (a.argmin_kind == BPL_ARGMIN_U8) am[kk] = static_cast<const uint8_t*>(amrow)[t];
-        else if (a.argmin_kind == BPL_ARGMIN_U16) am[kk] = static_cast<const uint16_t*>(amrow)[t];
-        else am[kk] = static_cast<int>(static_cast<const float*>(amrow)[t]);
-        sg += g[kk];
-        sa += accH[kk];
+      const bool valid = t < L;
+      int s = 0;
+      if (valid) {
+        if (a.argmin_kind == BPL_ARGMIN_U8) s = static_cast<const uint8_t*>(amrow)[t];
+        else if (a.argmin_kind == BPL_ARGMIN_U16) s = static_cast<const uint16_t*>(amrow)[t];
+        else s = static_cast<int>(static_cast<const float*>(amrow)[t]);
       }
+      am[kk] = s;
+      g[kk] = valid ? stg[a.lrow + t] : 0.0f;
+      // exp(m + log S) / S of the reference (:328-341) is exp(m) for a
+      // normalised message m = m_raw - log S
+      pr[kk] = valid ? expf(stg[t]) : 0.0f;
+      sU[kk] = (CROSS && valid) ? stg[2 * a.lrow + t] : 0.0f;
+      sD[kk] = (CROSS && valid) ? stg[3 * a.lrow + t] : 0.0f;
+      sg += g[kk];
+      sa += accH[kk];
     }
     // stage consumed: refill with step k + ns
     __syncwarp();
-    if (k + a.ns < nsteps) issue(k + a.ns);
+    if (k + a.ns < nsteps) issue(k + a.ns, st);
     if (!a.vec4) cp_async_commit();
 
     sg = warp_sum(sg);
@@ -313,8 +301,8 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       addH[kk] = (g[kk] - pr[kk] * sg) + (accH[kk] - pr[kk] * sa);
-      addU[kk] = cross ? sU[kk] + accU[kk] : 0.0f;
-      addD[kk] = cross ? sD[kk] + accD[kk] : 0.0f;
+      addU[kk] = CROSS ? sU[kk] + accU[kk] : 0.0f;
+      addD[kk] = CROSS ? sD[kk] + accD[kk] : 0.0f;
     }
 
     // Scatter by argmin.  Most labels share one argmin (the label of the
@@ -338,28 +326,29 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
     float dh = 0.0f, du = 0.0f, dd = 0.0f;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
-      if (lane + 32 * kk < L) {
-        if (am[kk] == gd) {
-          dh += addH[kk];
-          du += addU[kk];
-          dd += addD[kk];
-        } else {
-          atomicAdd(&rowH[am[kk]], addH[kk]);
-          if (cross) {
-            atomicAdd(&rowU[am[kk]], addU[kk]);
-            atomicAdd(&rowD[am[kk]], addD[kk]);
-          }
+      const bool v = lane + 32 * kk < L;
+      const bool dom = v && am[kk] == gd;
+      dh += dom ? addH[kk] : 0.0f;
+      if (CROSS) {
+        du += dom ? addU[kk] : 0.0f;
+        dd += dom ? addD[kk] : 0.0f;
+      }
+      if (v && !dom) {
+        atomicAdd(&rowH[am[kk]], addH[kk]);
+        if (CROSS) {
+          atomicAdd(&rowU[am[kk]], addU[kk]);
+          atomicAdd(&rowD[am[kk]], addD[kk]);
         }
       }
     }
     dh = warp_sum(dh);
-    if (cross) {
+    if (CROSS) {
       du = warp_sum(du);
       dd = warp_sum(dd);
     }
     if (lane == 0) {
       rowH[gd] += dh;  // no other lane touches label gd
-      if (cross) {
+      if (CROSS) {
         rowU[gd] += du;
         rowD[gd] += dd;
       }
@@ -376,25 +365,22 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
 #pragma unroll
       for (int kk = 0; kk < K; ++kk) {
         const int t = lane + 32 * kk;
-        if (t < L) {
-          const float tot = (addH[kk] + addU[kk]) + addD[kk];
-          const int ti = max(1, min(lv - 1, lv / 2 + (t - am[kk])));
+        const float tot = (t < L) ? (addH[kk] + addU[kk]) + addD[kk] : 0.0f;
+        const int ti = max(1, min(lv - 1, lv / 2 + (t - am[kk])));
 #pragma unroll
-          for (int bb = 1; bb < NB; ++bb)
-            if (bb < lv) bins[bb] += (ti == bb) ? tot : 0.0f;
-        }
+        for (int bb = 1; bb < NB; ++bb)
+          if (LV == 6 || LV == 8 || bb < lv) bins[bb] += (ti == bb) ? tot : 0.0f;
       }
       float ge = 0.0f;
 #pragma unroll
       for (int bb = 1; bb < NB; ++bb) {
-        if (bb < lv) {
+        if (LV == 6 || LV == 8 || bb < lv) {
           const float v = warp_sum(bins[bb]);
           ge += tile[bb * 33 + j] * v;
-          if (lane == bb && v != 0.0f)
-            atomicAdd(a.grad_jump + ((static_cast<int64_t>(nj) * 4 + fd) * a.Lv + bb) * HW + p, w * v);
+          if (lane == bb && v != 0.0f) atomicAdd(gjump_fd + static_cast<int64_t>(bb) * HW + p, w * v);
         }
       }
-      if (lane == 0 && ge != 0.0f) atomicAdd(a.grad_edge + (static_cast<int64_t>(ne) * 4 + fd) * HW + p, ge);
+      if (lane == 0 && ge != 0.0f) atomicAdd(gedge_fd + p, ge);
     } else {
       float ge = 0.0f;
 #pragma unroll
@@ -414,14 +400,14 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
       }
       if (VARIANT == BPL_LBP_SEM_GLOBAL) {
         ge = warp_sum(ge);
-        if (lane == 0) atomicAdd(a.grad_edge + (static_cast<int64_t>(ne) * 4 + fd) * HW + p, ge);
+        if (lane == 0) atomicAdd(gedge_fd + p, ge);
       }
     }
     __syncwarp();
 
     // read back the chain accumulators (and clear the rows for the next
     // step); grad_cost[p][s] receives rowH + rowU + rowD
-    float* gc = a.grad_cost + (static_cast<int64_t>(c.n) * HW + p) * L;
+    float* gc = gcost_n + static_cast<int64_t>(p) * L;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const int t = lane + 32 * kk;
@@ -429,7 +415,7 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
         accH[kk] = rowH[t];
         rowH[t] = 0.0f;
         float v = accH[kk];
-        if (cross) {
+        if (CROSS) {
           accU[kk] = rowU[t];
           accD[kk] = rowD[t];
           rowU[t] = 0.0f;
@@ -437,8 +423,7 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
           v = (v + accU[kk]) + accD[kk];
         }
         if (v != 0.0f) atomicAdd(gc + t, v);
-        if (a.phase == 0)
-          a.saved[((static_cast<int64_t>(c.n) * 2 + (c.db == UP ? 0 : 1)) * HW + p) * L + t] = accH[kk];
+        if (!CROSS) saved_out[static_cast<int64_t>(p) * L + t] = accH[kk];
       }
     }
 
@@ -450,6 +435,10 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
       }
     }
     __syncwarp();
+    if (++st == a.ns) {
+      st = 0;
+      par ^= 1u;
+    }
   }
 
   if (VARIANT == BPL_LBP_SEM_GLOBAL) {
@@ -475,14 +464,14 @@ int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
   const int per_warp = bwd::warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, V) * 4;
   const int wpb = std::max(1, std::min(4, (200 * 1024) / per_warp));
   const size_t smem = static_cast<size_t>(per_warp) * wpb;
-  auto kern = lbp_backward_kernel<K, V, LV>;
-  if (smem > 48 * 1024) {
-    if (static_cast<int>(smem) > max_smem_optin())
-      return set_error(BPL_ERR_UNSUPPORTED, "lbp_backward: shared memory %zu exceeds device limit", smem);
-    BPL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
-                 "cudaFuncSetAttribute");
-  }
   for (int phase = 0; phase < 2; ++phase) {
+    auto kern = (phase == 0) ? lbp_backward_kernel<K, V, LV, false> : lbp_backward_kernel<K, V, LV, true>;
+    if (smem > 48 * 1024) {
+      if (static_cast<int>(smem) > max_smem_optin())
+        return set_error(BPL_ERR_UNSUPPORTED, "lbp_backward: shared memory %zu exceeds device limit", smem);
+      BPL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+                   "cudaFuncSetAttribute");
+    }
     a.phase = phase;
     a.nchains = 2 * a.B * (phase == 0 ? a.W : a.H);
     const int blocks = (a.nchains + wpb - 1) / wpb;
