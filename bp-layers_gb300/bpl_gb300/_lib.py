@@ -24,6 +24,7 @@ SIGNATURES = {
     "bpl_lbp_forward": [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p] + [c_int] * 8 + [c_void_p],
     "bpl_lbp_backward_workspace_size": [c_int] * 4,
     "bpl_lbp_backward": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 5 + [ctypes.c_size_t] + [c_int] * 7 + [c_void_p],
+    "bpl_lbp_backward_noalloc": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 4 + [c_int] * 7 + [c_void_p],
 }
 _RESTYPE = {"bpl_status_string": ctypes.c_char_p, "bpl_last_error": ctypes.c_char_p,
             "bpl_lbp_backward_workspace_size": ctypes.c_size_t}

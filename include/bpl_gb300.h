@@ -120,6 +120,26 @@ int bpl_lbp_backward(int variant, const float* jump, const float* edge, const fl
                      size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
                      int edge_batch, void* stream);
 
+/*
+ * bpl_lbp_backward without device allocation.  No counterpart in the
+ * reference (its backward allocates scratch with at::zeros on every step).
+ * For hosts that cannot call cudaMalloc when they run the backward: device
+ * memory owned by another runtime's pool, a fixed budget set at start-up, or
+ * loops where an allocation's device synchronisation is not acceptable.
+ * Arguments and results are those of bpl_lbp_backward minus the workspace:
+ * the scratch is a fixed 16 MiB device array inside the library (held by
+ * every GPU that loads it), so B*2*H*W*L*4 must not exceed 16 MiB
+ * (BPL_ERR_INVALID_ARG otherwise).  All calls share that array: calls that
+ * overlap on the GPU race and must be serialised by the caller.  The first
+ * call on a device looks up the array's device address; make it before any
+ * stream capture.
+ */
+int bpl_lbp_backward_noalloc(int variant, const float* jump, const float* edge, const float* in_grad,
+                             const float* messages, const void* argmin, int argmin_kind,
+                             const float* scale, float* grad_cost, float* grad_jump, float* grad_edge,
+                             int B, int H, int W, int L, int Lv, int jump_batch, int edge_batch,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif
