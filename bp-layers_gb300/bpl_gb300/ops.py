@@ -173,3 +173,78 @@ def _timed(name, fn):
     b.record()
     _timing.setdefault(name, []).append((a, b))
     return r
+
+
+# ---------------------------------------------------------------------------
+# SAD cost volumes
+
+def sad_forward(f0: torch.Tensor, f1: torch.Tensor, min_disp: int, max_disp: int, step: float = 1.0,
+                out: torch.Tensor | None = None) -> torch.Tensor:
+    """Stereo SAD volume (B,H,W,D), bit-identical to the reference's
+    stereo_sad_forward (every batch item processed)."""
+    _check_input("f0", f0, dim=4)
+    _check_input("f1", f1, dim=4)
+    if f0.shape != f1.shape:
+        raise BplError("f0 and f1 must have the same shape")
+    B, C, H, W = f0.shape
+    D = int(lib().bpl_sad_volume_depth(int(min_disp), int(max_disp), float(step)))
+    if D < 1:
+        raise BplError("empty disparity range")
+    if out is None:
+        out = torch.empty((B, H, W, D), dtype=torch.float32, device=f0.device)
+    st = _timed("sad_forward", lambda: lib().bpl_sad_forward(
+        _ptr(f0), _ptr(f1), _ptr(out), B, C, H, W, int(min_disp), int(max_disp), float(step), _stream(f0)))
+    check(st, "bpl_sad_forward")
+    return out
+
+
+def sad_backward(f0: torch.Tensor, f1: torch.Tensor, min_disp: int, max_disp: int, in_grad: torch.Tensor,
+                 reference_channel_limit: bool = False):
+    """Gradients (df0, df1) of the SAD volume (step 1)."""
+    _check_input("f0", f0, dim=4)
+    _check_input("f1", f1, dim=4)
+    _check_input("in_grad", in_grad, dim=4)
+    B, C, H, W = f0.shape
+    D = int(max_disp) - int(min_disp) + 1
+    if tuple(in_grad.shape) != (B, H, W, D):
+        raise BplError(f"in_grad must be {(B, H, W, D)}, got {tuple(in_grad.shape)}")
+    df0 = torch.empty_like(f0)
+    df1 = torch.empty_like(f1)
+    st = _timed("sad_backward", lambda: lib().bpl_sad_backward(
+        _ptr(f0), _ptr(f1), _ptr(in_grad), _ptr(df0), _ptr(df1), B, C, H, W, int(min_disp), int(max_disp),
+        int(bool(reference_channel_limit)), _stream(f0)))
+    check(st, "bpl_sad_backward")
+    return df0, df1
+
+
+def flow_forward(f0: torch.Tensor, f1: torch.Tensor, sws: int, offset_u: int = 0, offset_v: int = 0,
+                 block_u: int = 0, block_v: int = 0):
+    """Flow max-projected SAD: (cv_u, cv_v, u_star, v_star), each (B,H,W,sws+1)."""
+    _check_input("f0", f0, dim=4)
+    _check_input("f1", f1, dim=4)
+    if f0.shape != f1.shape:
+        raise BplError("f0 and f1 must have the same shape")
+    B, C, H, W = f0.shape
+    K = int(sws) + 1
+    outs = [torch.empty((B, H, W, K), dtype=torch.float32, device=f0.device) for _ in range(4)]
+    st = _timed("flow_forward", lambda: lib().bpl_flow_forward(
+        _ptr(f0), _ptr(f1), *[_ptr(o) for o in outs], B, C, H, W, int(sws), int(offset_u), int(offset_v),
+        int(block_u), int(block_v), _stream(f0)))
+    check(st, "bpl_flow_forward")
+    return tuple(outs)
+
+
+def flow_backward(f0, f1, sws: int, in_grad_u, in_grad_v, u_star, v_star):
+    """Gradients (df0, df1) of the flow SAD."""
+    for nm, t in (("f0", f0), ("f1", f1)):
+        _check_input(nm, t, dim=4)
+    for nm, t in (("in_grad_u", in_grad_u), ("in_grad_v", in_grad_v), ("u_star", u_star), ("v_star", v_star)):
+        _check_input(nm, t, dim=4)
+    B, C, H, W = f0.shape
+    df0 = torch.empty_like(f0)
+    df1 = torch.empty_like(f1)
+    st = _timed("flow_backward", lambda: lib().bpl_flow_backward(
+        _ptr(f0), _ptr(f1), _ptr(in_grad_u), _ptr(in_grad_v), _ptr(u_star), _ptr(v_star), _ptr(df0), _ptr(df1),
+        B, C, H, W, int(sws), _stream(f0)))
+    check(st, "bpl_flow_backward")
+    return df0, df1

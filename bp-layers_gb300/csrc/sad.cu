@@ -1,0 +1,258 @@
+// Stereo SAD cost volume for sm_103a.
+//
+// Reference: ops/sad/src/stereo_sad_kernel.cu
+//   forward  :16-62   out[n,y,x,di] = sum_c |f0[n,c,y,x] - f1[n,c,y,x-d]|,
+//             d = (int)(di*step + min_disp), channels summed in order, 40
+//             where x-d is outside the image (:125), one thread per output
+//   backward :64-108  df0 = sum_d sign(f0-f1) g, df1 = -sum_d sign(.) g(x+d),
+//             gather form, d in increasing order, |diff| <= 1e-15 skipped
+//
+// GB300 design.  Forward: a block owns one row segment of TX pixels and all
+// D disparities.  The f0 segment (C x TX) and the f1 segment it can match
+// (C x (TX + dmax - dmin)) are staged in shared memory once; each thread
+// accumulates a 4-pixel x 8-disparity register tile over the channels in
+// order (two FP32 instructions per term, no FMA: bit-identical to the
+// reference), then writes its 8 disparities of each pixel as two 16-byte
+// stores.  FP32-issue bound (about 29 flop/byte at 376x1240x64x192), so no
+// TMA pipeline: one staged tile per block.
+// Backward: one thread per (channel, pixel) walks the disparities in the
+// reference order (additions of +-g in the same sequence: bit-identical); the
+// upstream-gradient rows are shared through L1 by the block's channels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "bpl_device.cuh"
+#include "bpl_internal.h"
+
+namespace bpl {
+namespace {
+
+constexpr int kTX = 64;          // pixels per block (forward)
+constexpr int kPX = 4;           // pixels per thread
+constexpr int kPD = 8;           // disparities per thread
+constexpr int kCChunk = 16;      // channels staged per pass
+
+struct SadArgs {
+  const float* f0;
+  const float* f1;
+  float* out;
+  int B, C, H, W, D;
+  int min_disp;
+  float step;
+  int unit_step;  // step == 1: d = di + min_disp
+  int dlo, dhi;   // smallest / largest disparity
+};
+
+__device__ __forceinline__ int disparity(const SadArgs& a, int di) {
+  if (a.unit_step) return di + a.min_disp;
+  // (d_idx * step) + min_disp in float, truncated (stereo_sad_kernel.cu:35)
+  return static_cast<int>(__fadd_rn(__fmul_rn(static_cast<float>(di), a.step), static_cast<float>(a.min_disp)));
+}
+
+// grid (ceil(W/kTX), H, B); block (D/kPD rounded up) x (kTX/kPX) threads
+__global__ void __launch_bounds__(512) sad_forward_kernel(SadArgs a) {
+  extern __shared__ __align__(16) float sm[];
+  const int n = blockIdx.z, y = blockIdx.y, x0 = blockIdx.x * kTX;
+  const int span = kTX + (a.dhi - a.dlo);      // f1 columns a block can match
+  const int spanp = (span + 3) & ~3;
+  float* s0 = sm;                              // [kCChunk][kTX]
+  float* s1 = sm + kCChunk * kTX;              // [kCChunk][spanp]
+  const int xb = x0 - a.dhi;                   // f1 column of s1[.][0]
+  const int ndg = (a.D + kPD - 1) / kPD;
+  const int tid = threadIdx.x;
+  const int nthreads = blockDim.x;
+  const int dg = tid % ndg;                    // disparity group
+  const int xg = tid / ndg;                    // pixel group
+  const bool active = xg < kTX / kPX;
+  const int64_t HW = static_cast<int64_t>(a.H) * a.W;
+  const float* f0 = a.f0 + static_cast<int64_t>(n) * a.C * HW + static_cast<int64_t>(y) * a.W;
+  const float* f1 = a.f1 + static_cast<int64_t>(n) * a.C * HW + static_cast<int64_t>(y) * a.W;
+
+  int dv[kPD];
+#pragma unroll
+  for (int q = 0; q < kPD; ++q) dv[q] = disparity(a, min(dg * kPD + q, a.D - 1));
+  float acc[kPX][kPD];
+#pragma unroll
+  for (int p = 0; p < kPX; ++p)
+#pragma unroll
+    for (int q = 0; q < kPD; ++q) acc[p][q] = 0.0f;
+
+  for (int c0 = 0; c0 < a.C; c0 += kCChunk) {
+    const int cn = min(kCChunk, a.C - c0);
+    __syncthreads();
+    for (int e = tid; e < cn * kTX; e += nthreads) {
+      const int cc = e / kTX, xx = e % kTX, x = x0 + xx;
+      s0[cc * kTX + xx] = (x < a.W) ? f0[(c0 + cc) * HW + x] : 0.0f;
+    }
+    for (int e = tid; e < cn * spanp; e += nthreads) {
+      const int cc = e / spanp, xx = e % spanp, x = xb + xx;
+      s1[cc * spanp + xx] = (x >= 0 && x < a.W && xx < span) ? f1[(c0 + cc) * HW + x] : 0.0f;
+    }
+    __syncthreads();
+    if (active) {
+      for (int cc = 0; cc < cn; ++cc) {
+        float v0[kPX];
+#pragma unroll
+        for (int p = 0; p < kPX; ++p) v0[p] = s0[cc * kTX + xg * kPX + p];
+        const float* r1 = s1 + cc * spanp;
+        // f1 column x - d sits at s1 index xl + dhi - d (xl: pixel in block)
+        if (a.unit_step) {
+          // d = d0 + q: the 4 x 8 tile reads 11 consecutive f1 values
+          // (indices below 0 of the last, partial disparity group land in
+          // the f0 tile and feed only outputs that are not stored)
+          const int base = xg * kPX + a.dhi - dv[0];
+          float v1[kPX + kPD - 1];
+#pragma unroll
+          for (int k = 0; k < kPX + kPD - 1; ++k) v1[k] = r1[base - (kPD - 1) + k];
+#pragma unroll
+          for (int p = 0; p < kPX; ++p)
+#pragma unroll
+            for (int q = 0; q < kPD; ++q)
+              acc[p][q] = __fadd_rn(acc[p][q], fabsf(__fsub_rn(v0[p], v1[p - q + kPD - 1])));
+        } else {
+#pragma unroll
+          for (int p = 0; p < kPX; ++p) {
+            const int xl = xg * kPX + p;
+#pragma unroll
+            for (int q = 0; q < kPD; ++q) {
+              const float v1 = r1[xl + a.dhi - dv[q]];
+              acc[p][q] = __fadd_rn(acc[p][q], fabsf(__fsub_rn(v0[p], v1)));
+            }
+          }
+        }
+      }
+    }
+  }
+  if (!active) return;
+  float* out = a.out + ((static_cast<int64_t>(n) * a.H + y) * a.W) * a.D;
+#pragma unroll
+  for (int p = 0; p < kPX; ++p) {
+    const int x = x0 + xg * kPX + p;
+    if (x >= a.W) continue;
+    float r[kPD];
+#pragma unroll
+    for (int q = 0; q < kPD; ++q) {
+      const int xm = x - dv[q];
+      r[q] = (xm >= 0 && xm < a.W) ? acc[p][q] : 40.0f;
+    }
+    float* o = out + static_cast<int64_t>(x) * a.D + dg * kPD;
+    if ((a.D % 4 == 0) && dg * kPD + kPD <= a.D) {
+      reinterpret_cast<float4*>(o)[0] = make_float4(r[0], r[1], r[2], r[3]);
+      reinterpret_cast<float4*>(o)[1] = make_float4(r[4], r[5], r[6], r[7]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < kPD; ++q)
+        if (dg * kPD + q < a.D) o[q] = r[q];
+    }
+  }
+}
+
+struct SadBwdArgs {
+  const float* f0;
+  const float* f1;
+  const float* g;
+  float* df0;
+  float* df1;
+  int B, C, H, W, D, min_disp, max_disp;
+  int channel_limit;
+};
+
+constexpr int kBX = 32;  // pixels per block (backward)
+
+// grid (ceil(W/kBX), H, B*ceil(C/cpb)); block kBX x cpb threads.  The
+// upstream-gradient rows are read through the L1 cache, shared by the
+// block's channels.
+__global__ void __launch_bounds__(256) sad_backward_kernel(SadBwdArgs a, int cpb) {
+  const int ncb = (a.C + cpb - 1) / cpb;
+  const int n = blockIdx.z / ncb;
+  const int c = (blockIdx.z % ncb) * cpb + threadIdx.y;
+  const int y = blockIdx.y;
+  const int x = blockIdx.x * kBX + threadIdx.x;
+  if (x >= a.W || c >= a.C || c >= a.channel_limit) return;
+  const int64_t HW = static_cast<int64_t>(a.H) * a.W;
+  const float* grow = a.g + ((static_cast<int64_t>(n) * a.H + y) * a.W) * a.D;
+  const float* r0 = a.f0 + (static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W;
+  const float* r1 = a.f1 + (static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W;
+  const float a0 = r0[x], b0 = r1[x];
+  float g0 = 0.0f, g1 = 0.0f;
+  for (int d = a.min_disp; d <= a.max_disp; ++d) {
+    const int idx = d - a.min_disp;
+    if (x - d >= 0 && x - d < a.W) {
+      const float diff = __fsub_rn(a0, __ldg(r1 + x - d));
+      const float gv = __ldg(grow + static_cast<int64_t>(x) * a.D + idx);
+      if (fabsf(diff) > 1e-15f) g0 = (diff > 0.0f) ? __fadd_rn(g0, gv) : __fsub_rn(g0, gv);
+    }
+    if (x + d >= 0 && x + d < a.W) {
+      const float diff1 = __fsub_rn(__ldg(r0 + x + d), b0);
+      const float gv = __ldg(grow + static_cast<int64_t>(x + d) * a.D + idx);
+      if (fabsf(diff1) > 1e-15f) g1 = (diff1 > 0.0f) ? __fsub_rn(g1, gv) : __fadd_rn(g1, gv);
+    }
+  }
+  a.df0[(static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W + x] = g0;
+  a.df1[(static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W + x] = g1;
+}
+
+}  // namespace
+}  // namespace bpl
+
+using namespace bpl;
+
+extern "C" int bpl_sad_volume_depth(int min_disp, int max_disp, float step) {
+  if (!(step > 0.0f)) return -1;
+  return static_cast<int>(static_cast<float>(max_disp - min_disp + 1) / step);
+}
+
+extern "C" int bpl_sad_forward(const float* f0, const float* f1, float* out, int B, int C, int H, int W,
+                               int min_disp, int max_disp, float step, void* stream) {
+  BPL_REQUIRE(f0 && f1 && out, "sad_forward: null pointer");
+  BPL_REQUIRE(B >= 1 && C >= 1 && H >= 1 && W >= 1, "sad_forward: bad shape");
+  BPL_REQUIRE(step > 0.0f, "sad_forward: step must be > 0");
+  const int D = bpl_sad_volume_depth(min_disp, max_disp, step);
+  BPL_REQUIRE(D >= 1, "sad_forward: empty disparity range");
+  SadArgs a{f0, f1, out, B, C, H, W, D, min_disp, step, step == 1.0f ? 1 : 0, 0, 0};
+  int lo = 1 << 30, hi = -(1 << 30);
+  for (int di = 0; di < D; ++di) {
+    const int d = a.unit_step ? di + min_disp
+                              : static_cast<int>(static_cast<float>(di) * step + static_cast<float>(min_disp));
+    lo = std::min(lo, d);
+    hi = std::max(hi, d);
+  }
+  // for fractional steps the host's float rounding may differ from the
+  // device's by one: widen the staged span by one on each side
+  a.dlo = a.unit_step ? lo : lo - 1;
+  a.dhi = a.unit_step ? hi : hi + 1;
+  BPL_REQUIRE(a.dhi - a.dlo <= 4096, "sad_forward: disparity span %d too large", a.dhi - a.dlo);
+  const int ndg = (D + kPD - 1) / kPD;
+  const int threads = ndg * (kTX / kPX);
+  BPL_REQUIRE(threads <= 1024, "sad_forward: D=%d too large (at most %d disparities)", D, 1024 / (kTX / kPX) * kPD);
+  const int span = kTX + (a.dhi - a.dlo);
+  const size_t smem = sizeof(float) * kCChunk * (kTX + ((span + 3) & ~3));
+  if (smem > 48 * 1024) {
+    BPL_REQUIRE(static_cast<int>(smem) <= max_smem_optin(), "sad_forward: disparity span too large");
+    BPL_CUDA_TRY(cudaFuncSetAttribute(sad_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem)), "cudaFuncSetAttribute");
+  }
+  dim3 grid((W + kTX - 1) / kTX, H, B);
+  sad_forward_kernel<<<grid, threads, smem, as_stream(stream)>>>(a);
+  BPL_CUDA_TRY(cudaGetLastError(), "sad_forward launch");
+  return BPL_OK;
+}
+
+extern "C" int bpl_sad_backward(const float* f0, const float* f1, const float* in_grad, float* df0, float* df1,
+                                int B, int C, int H, int W, int min_disp, int max_disp, int reference_channel_limit,
+                                void* stream) {
+  BPL_REQUIRE(f0 && f1 && in_grad && df0 && df1, "sad_backward: null pointer");
+  BPL_REQUIRE(B >= 1 && C >= 1 && H >= 1 && W >= 1 && max_disp >= min_disp, "sad_backward: bad shape");
+  const int D = max_disp - min_disp + 1;
+  SadBwdArgs a{f0, f1, in_grad, df0, df1, B, C, H, W, D, min_disp, max_disp, C};
+  // the reference launch covers only 4*ceil(D/4) channels (stereo_sad_kernel.cu:152-157)
+  if (reference_channel_limit) a.channel_limit = std::min(C, 4 * ((D + 3) / 4));
+  const int cpb = std::min(8, C);
+  BPL_CUDA_TRY(cudaMemsetAsync(df0, 0, sizeof(float) * B * C * H * W, as_stream(stream)), "sad_backward: memset");
+  BPL_CUDA_TRY(cudaMemsetAsync(df1, 0, sizeof(float) * B * C * H * W, as_stream(stream)), "sad_backward: memset");
+  dim3 grid((W + kBX - 1) / kBX, H, B * ((C + cpb - 1) / cpb));
+  sad_backward_kernel<<<grid, dim3(kBX, cpb), 0, as_stream(stream)>>>(a, cpb);
+  BPL_CUDA_TRY(cudaGetLastError(), "sad_backward launch");
+  return BPL_OK;
+}

@@ -120,6 +120,61 @@ int bpl_lbp_backward(int variant, const float* jump, const float* edge, const fl
                      size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
                      int edge_batch, void* stream);
 
+/* Disparity count D of the SAD volume: (int)((max_disp - min_disp + 1) / step)
+ * (ops/sad/src/stereo_sad_kernel.cu:122); -1 for a non-positive step. */
+int bpl_sad_volume_depth(int min_disp, int max_disp, float step);
+
+/*
+ * Stereo SAD cost volume.  Replaces cuda::stereo_sad_forward
+ * (ops/sad/src/stereo_sad_kernel.cu:116-136), bound as `forward`
+ * (ops/sad/src/stereo_sad.cpp:10-15).
+ * f0, f1 (B,C,H,W); out (B,H,W,D) with D = bpl_sad_volume_depth():
+ * out[n,y,x,di] = sum over c in order of |f0[n,c,y,x] - f1[n,c,y,x-d]|,
+ * d = (int)(di*step + min_disp), 40 where x-d is outside the image;
+ * bit-identical to the reference.  For a fractional step the reference's
+ * linear interpolation has weight 0 (d is an integer), so f1[x-d] is used.
+ * At most 512 disparities.
+ */
+int bpl_sad_forward(const float* f0, const float* f1, float* out, int B, int C, int H, int W,
+                    int min_disp, int max_disp, float step, void* stream);
+
+/*
+ * Gradient of the SAD volume (step 1).  Replaces cuda::stereo_sad_backward
+ * (ops/sad/src/stereo_sad_kernel.cu:138-165), bound as `backward`
+ * (ops/sad/src/stereo_sad.cpp:17-24).  in_grad (B,H,W,D); df0, df1 (B,C,H,W)
+ * are zero-filled by this call.  Bit-identical to the reference.  With
+ * reference_channel_limit != 0 only the first 4*ceil(D/4) channels receive a
+ * gradient, as in the reference launch (:152-157); 0 covers all channels.
+ */
+int bpl_sad_backward(const float* f0, const float* f1, const float* in_grad, float* df0, float* df1,
+                     int B, int C, int H, int W, int min_disp, int max_disp, int reference_channel_limit,
+                     void* stream);
+
+/*
+ * Flow max-projected SAD.  Replaces cuda::flow_mp_sad_forward
+ * (ops/flow_mp_sad/src/flow_mp_sad_kernel.cu:208-256), bound as `forward`
+ * (ops/flow_mp_sad/src/flow_mp_sad.cpp:10-16).  f0, f1 (B,C,H,W); outputs
+ * (B,H,W,K), K = sws+1: cv_u[u] = min over v of the window SAD, u_star[u] =
+ * argmin_v + block_v*sws, cv_v[v] = min over u, v_star[v] = argmin_u +
+ * block_u*sws (first index on ties; 40 outside the image); bit-identical to
+ * the reference.  Windows up to the shared-memory limit (K <= 226).
+ */
+int bpl_flow_forward(const float* f0, const float* f1, float* cv_u, float* cv_v, float* u_star,
+                     float* v_star, int B, int C, int H, int W, int sws, int offset_u, int offset_v,
+                     int block_u, int block_v, void* stream);
+
+/*
+ * Gradient of the flow SAD.  Replaces cuda::flow_mp_sad_backward
+ * (ops/flow_mp_sad/src/flow_mp_sad_kernel.cu:258-290), bound as `backward`
+ * (ops/flow_mp_sad/src/flow_mp_sad.cpp:18-30).  df0 is written (bit-identical
+ * to the reference), df1 is zero-filled and accumulated with float atomics.
+ * Like the reference, offsets are not applied (correct for block 0, zero
+ * offsets).
+ */
+int bpl_flow_backward(const float* f0, const float* f1, const float* in_grad_u, const float* in_grad_v,
+                      const float* u_star, const float* v_star, float* df0, float* df1, int B, int C,
+                      int H, int W, int sws, void* stream);
+
 /*
  * bpl_lbp_backward without device allocation.  No counterpart in the
  * reference (its backward allocates scratch with at::zeros on every step).
