@@ -220,6 +220,45 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
 
+    # ---- the same step with FP16 storage of cost and messages -----------------
+    fp16 = None
+    if not args.no_fp16:
+        mp16 = MessagePassing(dev, ITERS, L, DELTA, storage="fp16")
+        with torch.no_grad():
+            mp16._L1.fill_(0.1)
+            mp16._L2.fill_(0.5)
+
+        def step16(p, e, g):
+            beliefs, _ = mp16(p, e, None, None, None)
+            beliefs.backward(g)
+            return beliefs
+
+        for _ in range(args.warmup):
+            prob.grad = None
+            step16(prob, edge, upstream)
+        barrier()
+        h0 = torch.cuda.Event(enable_timing=True)
+        h1 = torch.cuda.Event(enable_timing=True)
+        with ops.timing() as tm16:
+            h0.record(stream)
+            for _ in range(args.steps):
+                prob.grad = None
+                b16 = step16(prob, edge, upstream)
+            h1.record(stream)
+            barrier()
+        ms16 = h0.elapsed_time(h1)
+        per16 = tm16.report()
+        prob.grad = None
+        b32 = step(prob, edge, upstream)
+        agree = float((b16.detach().argmax(-1) == b32.detach().argmax(-1)).float().mean().item())
+        f16 = per16.get("lbp_forward_f16", [])
+        bw16 = per16.get("lbp_backward_f16", [])
+        fp16 = {"value": updates_per_step() * args.steps * world / (ms16 / 1e3), "unit": UNIT,
+                "ms_per_step": ms16 / args.steps, "speedup_vs_fp32": ms_max / ms16,
+                "label_agreement_vs_fp32": agree,
+                "lbp_forward_pass_ms": sum(f16) / max(len(f16), 1), "lbp_backward_pass_ms": sum(bw16) / max(len(bw16), 1),
+                "bytes_per_update": {"forward": 11, "backward": 12}}
+
     U = updates_per_step()
     value = U * args.steps * world / (ms_max / 1e3)
     e2e_value = U * args.steps * world / (e2e_ms / 1e3)
@@ -252,6 +291,7 @@ def run_ours(args):
                       "forward_GBps_21B": U_pass * FWD_BYTES_PER_UPDATE / (fwd_ms / 1e3) / 1e9 if fwd else None,
                       "backward_GBps_17B": U_pass * BWD_BYTES_PER_UPDATE / (bwd_ms / 1e3) / 1e9 if bwd else None},
         "gpu_launches": args.steps * ITERS * 2 * 2,
+        "fp16": fp16,
         "clocks": clk.summary(),
     }
     traffic = os.path.join(ROOT, "profiles", "traffic.json")
@@ -368,6 +408,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp16", action="store_true", help="skip the FP16-storage leg")
     ap.add_argument("--ncu-case", action="store_true", help="small case for ncu captures")
     args = ap.parse_args()
     if args.ncu_case:

@@ -22,8 +22,10 @@ SIGNATURES = {
     "bpl_last_error": [],
     "bpl_read_device_error": [c_void_p],
     "bpl_lbp_forward": [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p] + [c_int] * 8 + [c_void_p],
+    "bpl_lbp_forward_f16": [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p] + [c_int] * 8 + [c_void_p],
     "bpl_lbp_backward_workspace_size": [c_int] * 4,
     "bpl_lbp_backward": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 5 + [ctypes.c_size_t] + [c_int] * 7 + [c_void_p],
+    "bpl_lbp_backward_f16": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 5 + [ctypes.c_size_t] + [c_int] * 7 + [c_void_p],
     "bpl_sad_volume_depth": [c_int, c_int, c_float],
     "bpl_sad_forward": [c_void_p] * 3 + [c_int] * 6 + [c_float, c_void_p],
     "bpl_sad_backward": [c_void_p] * 5 + [c_int] * 7 + [c_void_p],

@@ -93,8 +93,40 @@ class LBPMinSumFunction(torch.autograd.Function):
         return gc, ge, gm, None, g_aff, g_off
 
 
+class LBPMinSumFunctionF16(torch.autograd.Function):
+    """One LBP pass with FP16 storage of cost and messages (FP32 arithmetic).
+    forward(cost, cost_h, edge, messages_h, delta, affinities, offset) with
+    cost (N,H,W,L) float (the tensor the gradient is returned for), cost_h its
+    half copy with the label axis padded to a multiple of 8, messages_h
+    (N,4,H,W,Lp) half, updated in place like the float path."""
+
+    @staticmethod
+    def forward(ctx, cost, cost_h, edge, messages_h, delta, affinities, offset):
+        taps = pack_affinities(affinities, offset)
+        L = cost.shape[-1]
+        am_dtype = torch.uint8 if L <= 256 else torch.int16
+        messages_h, argmin, scale = ops.lbp_forward_f16(ops.LBP_STEREO, cost_h, taps, edge, messages_h, int(delta), L,
+                                                        argmin_dtype=am_dtype)
+        ctx.save_for_backward(taps, edge, messages_h, argmin, scale)
+        ctx.L = L
+        return messages_h
+
+    @staticmethod
+    def backward(ctx, in_grad):
+        taps, edge, messages_h, argmin, scale = ctx.saved_tensors
+        gc, gtaps, ge = ops.lbp_backward_f16(ops.LBP_STEREO, taps, edge, in_grad.contiguous(), messages_h, argmin,
+                                             scale, ctx.L)
+        g_aff, g_off = unpack_affinity_grad(gtaps)
+        return gc[..., :ctx.L], None, ge, in_grad, None, g_aff, g_off
+
+
 class MessagePassing(nn.Module):
-    """message_passing_op_cuda.py:95-177."""
+    """message_passing_op_cuda.py:95-177.  storage="fp16" keeps the cost
+    volume and the messages in half precision (label axis padded to a
+    multiple of 8) with FP32 arithmetic; the returned messages are then the
+    padded half tensor, each row stored relative to the minimum of h (a
+    constant per pixel and direction away from the reference's normalised
+    messages, which changes neither the beliefs' softmin nor a warm start)."""
 
     @property
     def L1(self):
@@ -113,13 +145,16 @@ class MessagePassing(nn.Module):
         elif value_L1 > value_L2:
             raise ValueError("L1 must be smaller than or equal L2!")
 
-    def __init__(self, device, max_iter, num_labels, delta, mode="min-sum"):
+    def __init__(self, device, max_iter, num_labels, delta, mode="min-sum", storage="fp32"):
         super().__init__()
         self.device = device
         self.max_iter = max_iter
         if mode != "min-sum":
             raise ValueError("Unknown message parsing mode " + mode)
+        if storage not in ("fp32", "fp16"):
+            raise ValueError("storage must be fp32 or fp16")
         self.mode = mode
+        self.storage = storage
         self._L1 = nn.Parameter(torch.tensor(0.1, device=device), requires_grad=True)
         self._L2 = nn.Parameter(torch.tensor(2.5, device=device), requires_grad=True)
         self.softmin = TemperatureSoftmin(dim=3, init_temp=1.0, device=device)
@@ -145,6 +180,18 @@ class MessagePassing(nn.Module):
         if offset is None:
             offset = torch.zeros((N, 4, H, W), device=dev)
         cost = -prob_vol
+        if self.storage == "fp16":
+            cost_h = ops.to_half_padded(cost.detach(), C)
+            if messages is None or messages.dtype != torch.float16:
+                m = torch.zeros((N, 4, H, W, ops.padded_labels(C)), dtype=torch.float16, device=dev)
+                if messages is not None:
+                    m[..., :C] = messages.detach()
+                messages = m.requires_grad_(True)
+            for _ in range(self.max_iter):
+                messages = LBPMinSumFunctionF16.apply(cost, cost_h, edge_weights, messages, self.delta, affinities,
+                                                      offset)
+            beliefs = messages[..., :C].float().sum(dim=1) + cost
+            return self.softmin.forward(beliefs), messages
         for _ in range(self.max_iter):
             messages = LBPMinSumFunction.apply(cost, edge_weights, messages, self.delta, affinities, offset)
         beliefs = messages.sum(dim=1) + cost

@@ -248,3 +248,102 @@ def flow_backward(f0, f1, sws: int, in_grad_u, in_grad_v, u_star, v_star):
         B, C, H, W, int(sws), _stream(f0)))
     check(st, "bpl_flow_backward")
     return df0, df1
+
+
+# ---------------------------------------------------------------------------
+# FP16 storage (label axis padded to a multiple of 8)
+
+def padded_labels(L: int) -> int:
+    return (int(L) + 7) & ~7
+
+
+def to_half_padded(t: torch.Tensor, L: int) -> torch.Tensor:
+    """Copy a (..., L) tensor into a zero-padded (..., Lp) half tensor."""
+    Lp = padded_labels(L)
+    out = torch.zeros(tuple(t.shape[:-1]) + (Lp,), dtype=torch.float16, device=t.device)
+    out[..., :L] = t
+    return out
+
+
+def normalised_f16_messages(messages_h: torch.Tensor, scale: torch.Tensor, L: int) -> torch.Tensor:
+    """(B,4,H,W,L) float log-normalised messages (the reference's form) from
+    the min-referenced half rows and the scale of lbp_forward_f16.  Rows no
+    sweep wrote (scale 0: the first sender of each scanline) are returned
+    as stored."""
+    shift = torch.where(scale > 0, torch.log(scale), torch.zeros_like(scale))
+    return messages_h[..., :L].float() - shift.unsqueeze(-1)
+
+
+def lbp_forward_f16(variant: int, cost_h: torch.Tensor, jump: torch.Tensor, edge: torch.Tensor,
+                    messages_h: torch.Tensor, delta: int, L: int, argmin_dtype=torch.uint8, argmin=None, scale=None):
+    """One LBP pass with FP16 storage.  cost_h (B,H,W,Lp) and messages_h
+    (B,4,H,W,Lp) half with Lp = padded_labels(L); messages updated in place.
+    The pixel variant takes jump (4,H,W,L,Lp) half, the stereo variant float
+    taps.  Returns (messages_h, argmin (B,4,H,W,Lp), scale).  Message rows
+    are stored relative to the minimum of h, with scale the sum of exp of the
+    row: the reference's log-normalised message is row - log(scale)
+    (normalised_f16_messages)."""
+    _check_input("cost_h", cost_h, dtype=torch.float16, dim=4)
+    _check_input("messages_h", messages_h, dtype=torch.float16, dim=5)
+    _check_input("edge", edge, dim=4)
+    Lp = padded_labels(L)
+    B, H, W, Lc = cost_h.shape
+    if Lc != Lp or tuple(messages_h.shape) != (B, 4, H, W, Lp):
+        raise BplError(f"FP16 tensors need the label axis padded to {Lp}")
+    Lv, jb = 0, 1
+    if variant == LBP_STEREO:
+        _check_input("jump", jump, dim=5)
+        Lv, jb = jump.shape[2], jump.shape[0]
+    elif variant == LBP_SEM_PIXEL:
+        _check_input("jump", jump, dtype=torch.float16, dim=5)
+        if tuple(jump.shape) != (4, H, W, L, Lp):
+            raise BplError(f"pixel jump must be (4,H,W,L,Lp) half, got {tuple(jump.shape)}")
+    else:
+        raise BplError("FP16 storage serves the stereo and pixel variants")
+    kind = _ARGMIN_KIND[argmin_dtype]
+    if argmin is None:
+        argmin = torch.zeros((B, 4, H, W, Lp), dtype=argmin_dtype, device=cost_h.device)
+    if scale is None:
+        scale = torch.zeros((B, 4, H, W), dtype=torch.float32, device=cost_h.device)
+    st = _timed("lbp_forward_f16", lambda: lib().bpl_lbp_forward_f16(
+        variant, _ptr(cost_h), _ptr(jump), _ptr(edge), _ptr(messages_h), _ptr(argmin), kind, _ptr(scale),
+        B, H, W, L, Lv, jb, edge.shape[0], int(delta), _stream(cost_h)))
+    check(st, "bpl_lbp_forward_f16")
+    return messages_h, argmin, scale
+
+
+def lbp_backward_f16(variant: int, jump, edge: torch.Tensor, in_grad_h: torch.Tensor, messages_h: torch.Tensor,
+                     argmin: torch.Tensor, scale: torch.Tensor, L: int, workspace: torch.Tensor | None = None):
+    """Reference adjoint for FP16-stored messages (padded label axis).
+    Returns (grad_cost (B,H,W,Lp) float, grad_jump, grad_edge)."""
+    _check_input("in_grad_h", in_grad_h, dtype=torch.float16, dim=5)
+    _check_input("messages_h", messages_h, dtype=torch.float16, dim=5)
+    _check_input("argmin", argmin, dtype=None, dim=5)
+    _check_input("scale", scale, dim=4)
+    _check_input("edge", edge, dim=4)
+    B, _, H, W, Lp = messages_h.shape
+    if Lp != padded_labels(L):
+        raise BplError("messages_h must have the padded label axis")
+    kind = _ARGMIN_KIND.get(argmin.dtype)
+    dev = messages_h.device
+    Lv, jb = 0, 1
+    if variant == LBP_STEREO:
+        _check_input("jump", jump, dim=5)
+        Lv, jb = jump.shape[2], jump.shape[0]
+        grad_jump = torch.empty((jb, 4, Lv, H, W), dtype=torch.float32, device=dev)
+        grad_edge = torch.empty(tuple(edge.shape), dtype=torch.float32, device=dev)
+    elif variant == LBP_SEM_PIXEL:
+        grad_jump = torch.empty((4, H, W, L, L), dtype=torch.float32, device=dev)
+        grad_edge = None
+    else:
+        raise BplError("FP16 storage serves the stereo and pixel variants")
+    grad_cost = torch.empty((B, H, W, Lp), dtype=torch.float32, device=dev)
+    need = lbp_backward_workspace_bytes(B, H, W, Lp)
+    if workspace is None or workspace.numel() * workspace.element_size() < need:
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    st = _timed("lbp_backward_f16", lambda: lib().bpl_lbp_backward_f16(
+        variant, _ptr(jump) if variant == LBP_STEREO else None, _ptr(edge), _ptr(in_grad_h), _ptr(messages_h),
+        _ptr(argmin), kind, _ptr(scale), _ptr(grad_cost), _ptr(grad_jump), _ptr(grad_edge), _ptr(workspace),
+        workspace.numel() * workspace.element_size(), B, H, W, L, Lv, jb, edge.shape[0], _stream(messages_h)))
+    check(st, "bpl_lbp_backward_f16")
+    return grad_cost, grad_jump, grad_edge

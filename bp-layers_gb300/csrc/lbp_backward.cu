@@ -9,11 +9,14 @@ extern "C" size_t bpl_lbp_backward_workspace_size(int B, int H, int W, int L) {
   return static_cast<size_t>(B) * 2 * H * W * L * sizeof(float);
 }
 
-extern "C" int bpl_lbp_backward(int variant, const float* jump, const float* edge, const float* in_grad,
-                                const float* messages, const void* argmin, int argmin_kind,
-                                const float* scale, float* grad_cost, float* grad_jump, float* grad_edge,
-                                void* workspace, size_t workspace_bytes, int B, int H, int W, int L,
-                                int Lv, int jump_batch, int edge_batch, void* stream) {
+namespace {
+
+// storage: 0 = float messages (reference layout), 1 = half messages with the
+// label axis padded to Lp = L rounded up to 8
+int lbp_backward_impl(int storage, int variant, const float* jump, const float* edge, const void* in_grad,
+                      const void* messages, const void* argmin, int argmin_kind, const float* scale,
+                      float* grad_cost, float* grad_jump, float* grad_edge, void* workspace, size_t workspace_bytes,
+                      int B, int H, int W, int L, int Lv, int jump_batch, int edge_batch, void* stream) {
   BPL_REQUIRE(variant >= 0 && variant <= 2, "lbp_backward: unknown variant %d", variant);
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1, "lbp_backward: bad shape B=%d H=%d W=%d", B, H, W);
   BPL_REQUIRE(H <= 65535 && W <= 65535, "lbp_backward: H and W must be <= 65535");
@@ -23,13 +26,16 @@ extern "C" int bpl_lbp_backward(int variant, const float* jump, const float* edg
   BPL_REQUIRE(variant == BPL_LBP_SEM_PIXEL || (jump && grad_edge), "lbp_backward: null jump/grad_edge");
   BPL_REQUIRE(argmin_kind >= BPL_ARGMIN_F32 && argmin_kind <= BPL_ARGMIN_U16, "lbp_backward: bad argmin kind");
   BPL_REQUIRE(edge_batch == 1 || edge_batch == B, "lbp_backward: edge batch %d must be 1 or B", edge_batch);
-  BPL_REQUIRE(workspace && workspace_bytes >= bpl_lbp_backward_workspace_size(B, H, W, L),
-              "lbp_backward: workspace of %zu bytes needed", bpl_lbp_backward_workspace_size(B, H, W, L));
+  const int Ls = (storage == 0) ? L : ((L + 7) & ~7);
+  BPL_REQUIRE(workspace && workspace_bytes >= bpl_lbp_backward_workspace_size(B, H, W, Ls),
+              "lbp_backward: workspace of %zu bytes needed", bpl_lbp_backward_workspace_size(B, H, W, Ls));
   if (variant == BPL_LBP_STEREO) {
     BPL_REQUIRE(Lv >= 2 && Lv <= 16, "lbp_backward: Lv=%d outside [2, 16]", Lv);
     BPL_REQUIRE(jump_batch == 1 || jump_batch == B, "lbp_backward: jump batch %d must be 1 or B", jump_batch);
   }
   if (variant == BPL_LBP_SEM_PIXEL) BPL_REQUIRE(L <= 96, "lbp_backward: pixel-pairwise variant supports L <= 96");
+  if (storage == 1)
+    BPL_REQUIRE(variant != BPL_LBP_SEM_GLOBAL, "lbp_backward_f16: FP16 storage serves the stereo and pixel variants");
 
   cudaStream_t s = as_stream(stream);
   const int64_t HW = static_cast<int64_t>(H) * W;
@@ -37,7 +43,7 @@ extern "C" int bpl_lbp_backward(int variant, const float* jump, const float* edg
   if (variant == BPL_LBP_STEREO) gj_elems = static_cast<size_t>(jump_batch) * 4 * Lv * HW;
   else if (variant == BPL_LBP_SEM_GLOBAL) gj_elems = static_cast<size_t>(B) * 4 * L * L;
   else gj_elems = static_cast<size_t>(4) * HW * L * L;
-  BPL_CUDA_TRY(cudaMemsetAsync(grad_cost, 0, sizeof(float) * B * HW * L, s), "lbp_backward: memset");
+  BPL_CUDA_TRY(cudaMemsetAsync(grad_cost, 0, sizeof(float) * B * HW * Ls, s), "lbp_backward: memset");
   BPL_CUDA_TRY(cudaMemsetAsync(grad_jump, 0, sizeof(float) * gj_elems, s), "lbp_backward: memset");
   if (grad_edge)
     BPL_CUDA_TRY(cudaMemsetAsync(grad_edge, 0, sizeof(float) * edge_batch * 4 * HW, s), "lbp_backward: memset");
@@ -57,18 +63,48 @@ extern "C" int bpl_lbp_backward(int variant, const float* jump, const float* edg
   a.H = H;
   a.W = W;
   a.L = L;
+  a.Ls = Ls;
   a.Lv = (variant == BPL_LBP_STEREO) ? Lv : 0;
   a.jb = jump_batch;
   a.eb = edge_batch;
   a.argmin_kind = argmin_kind;
-  a.lrow = bwd::a4(L);
-  a.vec4 = (L % 4 == 0) ? 1 : 0;
   const int am_size = (argmin_kind == BPL_ARGMIN_U8) ? 1 : (argmin_kind == BPL_ARGMIN_U16 ? 2 : 4);
-  a.am_bulk = (a.vec4 && (L * am_size) % 16 == 0) ? 1 : 0;
+  if (storage == 0) {
+    a.lrow = bwd::a4(L);
+    a.vec4 = (L % 4 == 0) ? 1 : 0;
+  } else {
+    a.lrow = Ls;
+    a.vec4 = 1;
+  }
+  a.am_bulk = (a.vec4 && (Ls * am_size) % 16 == 0) ? 1 : 0;
   a.ns = kBwdRingCpAsync;
+  if (storage == 1)
+    return (variant == BPL_LBP_STEREO) ? lbp_backward_stereo_f16(a, s) : lbp_backward_sem_pixel_f16(a, s);
   switch (variant) {
     case BPL_LBP_STEREO: return lbp_backward_stereo(a, s);
     case BPL_LBP_SEM_GLOBAL: return lbp_backward_sem_global(a, s);
     default: return lbp_backward_sem_pixel(a, s);
   }
+}
+
+}  // namespace
+
+extern "C" int bpl_lbp_backward(int variant, const float* jump, const float* edge, const float* in_grad,
+                                const float* messages, const void* argmin, int argmin_kind,
+                                const float* scale, float* grad_cost, float* grad_jump, float* grad_edge,
+                                void* workspace, size_t workspace_bytes, int B, int H, int W, int L,
+                                int Lv, int jump_batch, int edge_batch, void* stream) {
+  return lbp_backward_impl(0, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
+                           grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
+                           stream);
+}
+
+extern "C" int bpl_lbp_backward_f16(int variant, const float* jump, const float* edge, const void* in_grad,
+                                    const void* messages, const void* argmin, int argmin_kind, const float* scale,
+                                    float* grad_cost, float* grad_jump, float* grad_edge, void* workspace,
+                                    size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
+                                    int edge_batch, void* stream) {
+  return lbp_backward_impl(1, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
+                           grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
+                           stream);
 }

@@ -25,6 +25,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cuda_fp16.h>
+
 #include <algorithm>
 
 #include "bpl_device.cuh"
@@ -32,11 +34,15 @@
 
 namespace bpl {
 
+// Messages and their upstream gradient are stored as T (float, or __half
+// with the label axis padded to Ls = L rounded up to 8); everything else is
+// float.  Ls is the label stride of messages, in_grad, argmin, grad_cost and
+// the workspace.
 struct BwdArgs {
   const float* jump;
   const float* edge;
-  const float* in_grad;
-  const float* msgs;
+  const void* in_grad;
+  const void* msgs;
   const void* argmin;
   const float* scale;
   float* grad_cost;
@@ -44,6 +50,7 @@ struct BwdArgs {
   float* grad_edge;
   float* saved;  // workspace (B,2,H,W,L): slot 0 = UP chain, slot 1 = DOWN chain
   int B, H, W, L, Lv, jb, eb;
+  int Ls;
   int argmin_kind;
   int phase;  // 0: DOWN+UP over columns, 1: LEFT+RIGHT over rows
   int nchains;
@@ -59,14 +66,14 @@ namespace bwd {
 
 __host__ __device__ inline int a4(int v) { return (v + 3) & ~3; }
 
-// rows per stage: messages, in_grad, saved UP, saved DOWN (floats) and the
-// argmin row (up to 4 bytes per label)
-__host__ __device__ inline int stage_floats(int lrow) { return 5 * lrow; }
+// rows per stage: messages and in_grad (T), saved UP and saved DOWN (float)
+// and the argmin row (up to 4 bytes per label), each lrow labels long
+__host__ __device__ inline int stage_floats(int lrow, int tsize) { return 2 * lrow * tsize / 4 + 3 * lrow; }
 
 __host__ __device__ inline int tile_floats(int Lv) { return a4(2 * (Lv + 2) * 33); }
 
-__host__ __device__ inline int warp_smem_floats(int K, int ns, int lrow, int Lv, int L, int variant) {
-  const int ring = ns * stage_floats(lrow);
+__host__ __device__ inline int warp_smem_floats(int K, int ns, int lrow, int Lv, int L, int variant, int tsize) {
+  const int ring = ns * stage_floats(lrow, tsize);
   const int bars = 2 * a4(ns);
   const int rows = 3 * 32 * K;                      // scatter rows of acc HOR/UP/DOWN
   const int jacc = (variant == BPL_LBP_SEM_GLOBAL) ? a4(L * L) : 0;
@@ -82,10 +89,10 @@ struct Smem {
 };
 
 template <int K>
-__device__ __forceinline__ Smem carve(float* base, const BwdArgs& a, int variant) {
+__device__ __forceinline__ Smem carve(float* base, const BwdArgs& a, int variant, int tsize) {
   Smem s;
   s.ring = base;
-  float* p = base + a4(a.ns * stage_floats(a.lrow));
+  float* p = base + a4(a.ns * stage_floats(a.lrow, tsize));
   s.bars = reinterpret_cast<uint64_t*>(p);
   p += 2 * a4(a.ns);
   s.rows = p;
@@ -101,7 +108,14 @@ __device__ __forceinline__ Smem carve(float* base, const BwdArgs& a, int variant
 // LV: number of stereo jump taps when known at compile time (6 or 8), 16 for
 // any Lv <= 16 given at run time, 0 for the semantic variants.  CROSS: the
 // horizontal phase (LEFT+RIGHT, with the vertical chains' saved gradients).
-template <int K, int VARIANT, int LV, bool CROSS>
+template <typename T>
+__device__ __forceinline__ float bldf(T v);
+template <>
+__device__ __forceinline__ float bldf<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float bldf<__half>(__half v) { return __half2float(v); }
+
+template <int K, int VARIANT, int LV, bool CROSS, typename T>
 __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   using namespace bwd;
   extern __shared__ __align__(16) float smem[];
@@ -110,12 +124,13 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   const int chain_id = blockIdx.x * (blockDim.x >> 5) + wib;
   if (chain_id >= a.nchains) return;
 
-  const int per_warp = warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, VARIANT);
-  Smem sm = carve<K>(smem + static_cast<int64_t>(wib) * per_warp, a, VARIANT);
+  const int per_warp = warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, VARIANT, sizeof(T));
+  Smem sm = carve<K>(smem + static_cast<int64_t>(wib) * per_warp, a, VARIANT, sizeof(T));
 
   const int L = a.L;
+  const int Ls = a.Ls;
   const int64_t HW = static_cast<int64_t>(a.H) * a.W;
-  const int64_t HWL = HW * L;
+  const int64_t HWL = HW * Ls;
   // chain: sender of step k is pin0 + k*dpin (pixel index within the image),
   // its receiver is dq further
   int n, db, pin0, dpin, dq, nsteps;
@@ -144,8 +159,8 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   const int nj = (a.jb == 1) ? 0 : n;
   const int ne = (a.eb == 1) ? 0 : n;
   const uint32_t am_size = (a.argmin_kind == BPL_ARGMIN_U8) ? 1u : (a.argmin_kind == BPL_ARGMIN_U16 ? 2u : 4u);
-  const float* msgs_db = a.msgs + (static_cast<int64_t>(n) * 4 + db) * HWL;
-  const float* grad_db = a.in_grad + (static_cast<int64_t>(n) * 4 + db) * HWL;
+  const T* msgs_db = static_cast<const T*>(a.msgs) + (static_cast<int64_t>(n) * 4 + db) * HWL;
+  const T* grad_db = static_cast<const T*>(a.in_grad) + (static_cast<int64_t>(n) * 4 + db) * HWL;
   const uint8_t* am_db = static_cast<const uint8_t*>(a.argmin) + (static_cast<int64_t>(n) * 4 + db) * HWL * am_size;
   const float* saved_up = a.saved + (static_cast<int64_t>(n) * 2 + 0) * HWL;
   const float* saved_dn = a.saved + (static_cast<int64_t>(n) * 2 + 1) * HWL;
@@ -161,7 +176,7 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   // sweeps: the DOWN chain's row 0 and the UP chain's row H-1
   if (!CROSS) {
     const int x = (chain_id >> 1) % a.W;
-    float* dst = saved_out + (static_cast<int64_t>((db == DOWN) ? 0 : a.H - 1) * a.W + x) * L;
+    float* dst = saved_out + (static_cast<int64_t>((db == DOWN) ? 0 : a.H - 1) * a.W + x) * Ls;
     for (int t = lane; t < L; t += 32) dst[t] = 0.0f;
   }
   if (nsteps <= 0) return;
@@ -171,30 +186,35 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   if (VARIANT == BPL_LBP_SEM_GLOBAL)
     for (int t = lane; t < L * L; t += 32) sm.jacc[t] = 0.0f;
 
+  // stage rows: messages (T), in_grad (T), saved UP, saved DOWN (float), argmin
+  const int lr = a.lrow;
+  const int tfl = lr * static_cast<int>(sizeof(T)) / 4;  // floats per T row
   auto issue = [&](int k, int st) {
-    float* dst = sm.ring + st * stage_floats(a.lrow);
-    const int64_t qo = static_cast<int64_t>(pin0 + k * dpin + dq) * L;
+    float* dst = sm.ring + st * stage_floats(lr, sizeof(T));
+    const int64_t qo = static_cast<int64_t>(pin0 + k * dpin + dq) * Ls;
     if (a.vec4) {
       if (lane == 0) {
-        const uint32_t rb = static_cast<uint32_t>(L) * 4u;
-        const uint32_t ab = a.am_bulk ? static_cast<uint32_t>(L) * am_size : 0u;
+        const uint32_t rt = static_cast<uint32_t>(Ls) * static_cast<uint32_t>(sizeof(T));
+        const uint32_t rf = static_cast<uint32_t>(Ls) * 4u;
+        const uint32_t ab = a.am_bulk ? static_cast<uint32_t>(Ls) * am_size : 0u;
         fence_proxy_async();
-        mbar_arrive_expect_tx(&sm.bars[st], (CROSS ? 4u : 2u) * rb + ab);
-        bulk_g2s(dst, msgs_db + qo, rb, &sm.bars[st]);
-        bulk_g2s(dst + a.lrow, grad_db + qo, rb, &sm.bars[st]);
+        mbar_arrive_expect_tx(&sm.bars[st], 2u * rt + (CROSS ? 2u * rf : 0u) + ab);
+        bulk_g2s(dst, msgs_db + qo, rt, &sm.bars[st]);
+        bulk_g2s(dst + tfl, grad_db + qo, rt, &sm.bars[st]);
         if (CROSS) {
-          bulk_g2s(dst + 2 * a.lrow, saved_up + qo, rb, &sm.bars[st]);
-          bulk_g2s(dst + 3 * a.lrow, saved_dn + qo, rb, &sm.bars[st]);
+          bulk_g2s(dst + 2 * tfl, saved_up + qo, rf, &sm.bars[st]);
+          bulk_g2s(dst + 2 * tfl + lr, saved_dn + qo, rf, &sm.bars[st]);
         }
-        if (a.am_bulk) bulk_g2s(dst + 4 * a.lrow, am_db + qo * am_size, ab, &sm.bars[st]);
+        if (a.am_bulk) bulk_g2s(dst + 2 * tfl + 2 * lr, am_db + qo * am_size, ab, &sm.bars[st]);
       }
-    } else {
+    } else if constexpr (sizeof(T) == 4) {
+      // rows not 16-byte sized (float storage only; half rows are padded)
       for (int t = lane; t < L; t += 32) {
         cp_async4(dst + t, msgs_db + qo + t);
-        cp_async4(dst + a.lrow + t, grad_db + qo + t);
+        cp_async4(dst + tfl + t, grad_db + qo + t);
         if (CROSS) {
-          cp_async4(dst + 2 * a.lrow + t, saved_up + qo + t);
-          cp_async4(dst + 3 * a.lrow + t, saved_dn + qo + t);
+          cp_async4(dst + 2 * tfl + t, saved_up + qo + t);
+          cp_async4(dst + 2 * tfl + lr + t, saved_dn + qo + t);
         }
       }
     }
@@ -243,7 +263,7 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   float* rowH = sm.rows;
   float* rowU = sm.rows + 32 * K;
   float* rowD = sm.rows + 64 * K;
-  const int sf = stage_floats(a.lrow);
+  const int sf = stage_floats(lr, sizeof(T));
 
   bool failed = false;
   int st = 0;
@@ -254,7 +274,7 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
     const int b = k >> 5;
     const float* tile = sm.tile + (b & 1) * (trow * 33);
     const float* stg = sm.ring + st * sf;
-    const int64_t qo = static_cast<int64_t>(p + dq) * L;
+    const int64_t qo = static_cast<int64_t>(p + dq) * Ls;
 
     if (a.vec4) {
       const bool ok = mbar_wait_bounded(&sm.bars[st], par);
@@ -265,10 +285,15 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
     }
 
     const float w = tile[a.Lv * 33 + j];
+    const float inv_s = (sizeof(T) == 4) ? 1.0f : __frcp_rn(tile[(a.Lv + 1) * 33 + j]);
     float g[K], pr[K], sU[K], sD[K];
     int am[K];
     float sg = 0.0f, sa = 0.0f;
-    const void* amrow = a.am_bulk ? static_cast<const void*>(stg + 4 * a.lrow)
+    const T* m_row = reinterpret_cast<const T*>(stg);
+    const T* g_row = reinterpret_cast<const T*>(stg + tfl);
+    const float* su_row = stg + 2 * tfl;
+    const float* sd_row = su_row + lr;
+    const void* amrow = a.am_bulk ? static_cast<const void*>(sd_row + lr)
                                   : static_cast<const void*>(am_db + qo * am_size);
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
@@ -281,12 +306,14 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
         else s = static_cast<int>(static_cast<const float*>(amrow)[t]);
       }
       am[kk] = s;
-      g[kk] = valid ? stg[a.lrow + t] : 0.0f;
+      g[kk] = valid ? bldf<T>(g_row[t]) : 0.0f;
       // exp(m + log S) / S of the reference (:328-341) is exp(m) for a
       // normalised message m = m_raw - log S
-      pr[kk] = valid ? expf(stg[t]) : 0.0f;
-      sU[kk] = (CROSS && valid) ? stg[2 * a.lrow + t] : 0.0f;
-      sD[kk] = (CROSS && valid) ? stg[3 * a.lrow + t] : 0.0f;
+      // normalised message m = m_raw - log S; half rows hold m_raw - min h
+      // with their scale the sum of exp of the row, so exp(m) = exp(row) / scale
+      pr[kk] = valid ? (sizeof(T) == 4 ? expf(bldf<T>(m_row[t])) : __expf(bldf<T>(m_row[t])) * inv_s) : 0.0f;
+      sU[kk] = (CROSS && valid) ? su_row[t] : 0.0f;
+      sD[kk] = (CROSS && valid) ? sd_row[t] : 0.0f;
       sg += g[kk];
       sa += accH[kk];
     }
@@ -407,7 +434,7 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
 
     // read back the chain accumulators (and clear the rows for the next
     // step); grad_cost[p][s] receives rowH + rowU + rowD
-    float* gc = gcost_n + static_cast<int64_t>(p) * L;
+    float* gc = gcost_n + static_cast<int64_t>(p) * Ls;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const int t = lane + 32 * kk;
@@ -423,7 +450,7 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
           v = (v + accU[kk]) + accD[kk];
         }
         if (v != 0.0f) atomicAdd(gc + t, v);
-        if (!CROSS) saved_out[static_cast<int64_t>(p) * L + t] = accH[kk];
+        if (!CROSS) saved_out[static_cast<int64_t>(p) * Ls + t] = accH[kk];
       }
     }
 
@@ -458,14 +485,14 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   if (!a.vec4) cp_async_wait<0>();
 }
 
-template <int K, int V, int LV>
+template <int K, int V, int LV, typename T>
 int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
   BwdArgs a = a0;
-  const int per_warp = bwd::warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, V) * 4;
+  const int per_warp = bwd::warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, V, sizeof(T)) * 4;
   const int wpb = std::max(1, std::min(4, (200 * 1024) / per_warp));
   const size_t smem = static_cast<size_t>(per_warp) * wpb;
   for (int phase = 0; phase < 2; ++phase) {
-    auto kern = (phase == 0) ? lbp_backward_kernel<K, V, LV, false> : lbp_backward_kernel<K, V, LV, true>;
+    auto kern = (phase == 0) ? lbp_backward_kernel<K, V, LV, false, T> : lbp_backward_kernel<K, V, LV, true, T>;
     if (smem > 48 * 1024) {
       if (static_cast<int>(smem) > max_smem_optin())
         return set_error(BPL_ERR_UNSUPPORTED, "lbp_backward: shared memory %zu exceeds device limit", smem);
@@ -481,34 +508,36 @@ int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
   return BPL_OK;
 }
 
-template <int V, int LV>
+template <int V, int LV, typename T = float>
 int dispatch_bwd(const BwdArgs& a, cudaStream_t s) {
   const int k = (a.L + 31) / 32;
   if constexpr (V == BPL_LBP_SEM_PIXEL) {
-    if (k == 1) return launch_bwd_k<1, V, LV>(a, s);
-    if (k == 2) return launch_bwd_k<2, V, LV>(a, s);
-    return launch_bwd_k<3, V, LV>(a, s);
+    if (k == 1) return launch_bwd_k<1, V, LV, T>(a, s);
+    if (k == 2) return launch_bwd_k<2, V, LV, T>(a, s);
+    return launch_bwd_k<3, V, LV, T>(a, s);
   }
   switch (k) {
-    case 1: return launch_bwd_k<1, V, LV>(a, s);
-    case 2: return launch_bwd_k<2, V, LV>(a, s);
-    case 3: return launch_bwd_k<3, V, LV>(a, s);
-    case 4: return launch_bwd_k<4, V, LV>(a, s);
-    case 5: return launch_bwd_k<5, V, LV>(a, s);
-    case 6: return launch_bwd_k<6, V, LV>(a, s);
-    case 7: return launch_bwd_k<7, V, LV>(a, s);
-    case 8: return launch_bwd_k<8, V, LV>(a, s);
+    case 1: return launch_bwd_k<1, V, LV, T>(a, s);
+    case 2: return launch_bwd_k<2, V, LV, T>(a, s);
+    case 3: return launch_bwd_k<3, V, LV, T>(a, s);
+    case 4: return launch_bwd_k<4, V, LV, T>(a, s);
+    case 5: return launch_bwd_k<5, V, LV, T>(a, s);
+    case 6: return launch_bwd_k<6, V, LV, T>(a, s);
+    case 7: return launch_bwd_k<7, V, LV, T>(a, s);
+    case 8: return launch_bwd_k<8, V, LV, T>(a, s);
     default:
-      if (k <= 12) return launch_bwd_k<12, V, LV>(a, s);
-      if (k <= 16) return launch_bwd_k<16, V, LV>(a, s);
-      if (k <= 24) return launch_bwd_k<24, V, LV>(a, s);
-      return launch_bwd_k<32, V, LV>(a, s);
+      if (k <= 12) return launch_bwd_k<12, V, LV, T>(a, s);
+      if (k <= 16) return launch_bwd_k<16, V, LV, T>(a, s);
+      if (k <= 24) return launch_bwd_k<24, V, LV, T>(a, s);
+      return launch_bwd_k<32, V, LV, T>(a, s);
   }
 }
 
 int lbp_backward_stereo_lv6(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_stereo_lv8(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_stereo(const BwdArgs& a, cudaStream_t s);
+int lbp_backward_stereo_f16(const BwdArgs& a, cudaStream_t s);
+int lbp_backward_sem_pixel_f16(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_sem_global(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_sem_pixel(const BwdArgs& a, cudaStream_t s);
 

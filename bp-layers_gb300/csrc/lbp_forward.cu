@@ -8,10 +8,12 @@ __device__ int g_bpl_error = 0;
 
 using namespace bpl;
 
-extern "C" int bpl_lbp_forward(int variant, const float* cost, const float* jump, const float* edge,
-                               float* messages, void* argmin, int argmin_kind, float* scale, int B,
-                               int H, int W, int L, int Lv, int jump_batch, int edge_batch, int delta,
-                               void* stream) {
+namespace {
+
+// storage: 0 = float (reference layout), 1 = half (label stride rounded to 8)
+int lbp_forward_impl(int storage, int variant, const void* cost, const void* jump, const float* edge,
+                     void* messages, void* argmin, int argmin_kind, float* scale, int B, int H, int W, int L,
+                     int Lv, int jump_batch, int edge_batch, int delta, void* stream) {
   BPL_REQUIRE(variant >= 0 && variant <= 2, "lbp_forward: unknown variant %d", variant);
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1, "lbp_forward: bad shape B=%d H=%d W=%d", B, H, W);
   BPL_REQUIRE(H <= 65535 && W <= 65535, "lbp_forward: H and W must be <= 65535");
@@ -28,6 +30,8 @@ extern "C" int bpl_lbp_forward(int variant, const float* cost, const float* jump
   }
   if (variant == BPL_LBP_SEM_PIXEL)
     BPL_REQUIRE(L <= 96, "lbp_forward: pixel-pairwise variant supports L <= 96");
+  if (storage == 1)
+    BPL_REQUIRE(variant != BPL_LBP_SEM_GLOBAL, "lbp_forward_f16: FP16 storage serves the stereo and pixel variants");
 
   FwdArgs a{};
   a.cost = cost;
@@ -46,17 +50,45 @@ extern "C" int bpl_lbp_forward(int variant, const float* cost, const float* jump
   a.delta = delta;
   a.argmin_kind = argmin_kind;
   a.lrow = align4(L);
-  a.lmat = 0;
-  a.vec4 = (L % 4 == 0) ? 1 : 0;
-  if (variant == BPL_LBP_SEM_PIXEL) {
-    a.lmat = align4(L * L);
-    a.vec4 = a.vec4 && ((L * L) % 4 == 0);
+  if (storage == 0) {
+    a.Ls = L;
+    a.Lm = L;
+    a.lmat = 0;
+    a.vec4 = (L % 4 == 0) ? 1 : 0;
+    if (variant == BPL_LBP_SEM_PIXEL) {
+      a.lmat = align4(L * L);
+      a.vec4 = a.vec4 && ((L * L) % 4 == 0);
+    }
+  } else {
+    a.Ls = (L + 7) & ~7;
+    a.Lm = a.Ls;
+    a.lmat = (variant == BPL_LBP_SEM_PIXEL) ? L * a.Lm : 0;
+    a.vec4 = 1;
   }
   a.ns = a.vec4 ? 4 : kRingCpAsync;
   cudaStream_t s = as_stream(stream);
+  if (storage == 1) return (variant == BPL_LBP_STEREO) ? lbp_forward_stereo_f16(a, s) : lbp_forward_sem_pixel_f16(a, s);
   switch (variant) {
     case BPL_LBP_STEREO: return lbp_forward_stereo(a, s);
     case BPL_LBP_SEM_GLOBAL: return lbp_forward_sem_global(a, s);
     default: return lbp_forward_sem_pixel(a, s);
   }
+}
+
+}  // namespace
+
+extern "C" int bpl_lbp_forward(int variant, const float* cost, const float* jump, const float* edge,
+                               float* messages, void* argmin, int argmin_kind, float* scale, int B,
+                               int H, int W, int L, int Lv, int jump_batch, int edge_batch, int delta,
+                               void* stream) {
+  return lbp_forward_impl(0, variant, cost, jump, edge, messages, argmin, argmin_kind, scale, B, H, W, L, Lv,
+                          jump_batch, edge_batch, delta, stream);
+}
+
+extern "C" int bpl_lbp_forward_f16(int variant, const void* cost, const void* jump, const float* edge,
+                                   void* messages, void* argmin, int argmin_kind, float* scale, int B, int H,
+                                   int W, int L, int Lv, int jump_batch, int edge_batch, int delta,
+                                   void* stream) {
+  return lbp_forward_impl(1, variant, cost, jump, edge, messages, argmin, argmin_kind, scale, B, H, W, L, Lv,
+                          jump_batch, edge_batch, delta, stream);
 }

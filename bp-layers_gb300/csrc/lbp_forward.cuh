@@ -25,6 +25,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cuda_fp16.h>
+
 #include <algorithm>
 
 #include "bpl_crmath.cuh"
@@ -46,20 +48,26 @@ constexpr int kHsPad = 4;
 // the per-label work dominates the per-step reductions).
 constexpr int kSplitChainsPerSm = 0;
 
+// Storage type T of cost, messages (and the pixel-pairwise matrices): float
+// (reference layout, bit-exact) or __half (FP16 storage, FP32 arithmetic).
+// Rows of L labels are stored with a label stride Ls >= L (Ls = L for float;
+// L rounded up to 8 for __half, so every row is 16-byte sized).
 struct FwdArgs {
-  const float* cost;
-  const float* jump;
+  const void* cost;
+  const void* jump;
   const float* edge;
-  float* msgs;
+  void* msgs;
   void* argmin;
   float* scale;
   int B, H, W, L, Lv, jb, eb, delta;
+  int Ls;     // label stride of cost / messages / argmin rows
+  int Lm;     // row stride of the pixel-pairwise matrices (pixel variant)
   int argmin_kind;
   int phase;  // 0: RIGHT+LEFT over rows, 1: DOWN+UP over columns
   int nchains;
   int ns;     // ring depth
-  int lrow;   // floats per ring row (L rounded up to 4)
-  int lmat;   // floats of the per-pixel pairwise matrix in a stage (pixel variant), else 0
+  int lrow;   // unused
+  int lmat;   // elements of the per-pixel pairwise matrix in a stage (pixel variant), else 0
   int vec4;   // rows are 16-byte sized: use bulk copies
 };
 
@@ -71,6 +79,14 @@ __device__ __forceinline__ float norm_exp(float m, const float* ehi, const float
   float y;
   if (!crm::exp_fast(m, y, ehi, elo)) y = static_cast<float>(exp(static_cast<double>(m)));
   return y;
+}
+// exp of the normalisation: the exact evaluation above (float storage) or
+// the hardware approximation (half storage, not bit-exact by design)
+template <bool EXACT>
+__device__ __forceinline__ bool exp_try(float x, float& y, const float* ehi, const float* elo) {
+  if (EXACT) return crm::exp_fast(x, y, ehi, elo);
+  y = __expf(x);
+  return true;
 }
 __device__ __forceinline__ float norm_log(float sum) {
   float y;
@@ -88,13 +104,31 @@ __device__ __forceinline__ float norm_log(float sum) {
 //              taps tile 2 x (Lv+1) x 33 floats.
 __host__ __device__ inline int align4(int v) { return (v + 3) & ~3; }
 
-__host__ __device__ inline int stage_floats(int lrow, int lmat) { return 3 * lrow + lmat; }
+// elements of T per ring stage
+__host__ __device__ inline int stage_elems(int lrow, int lmat) { return 3 * lrow + lmat; }
 
 __host__ __device__ inline int chain_smem_floats(int K) { return align4(32 * K + 2 * kHsPad) + 32 * K + 16; }
 
-__host__ __device__ inline int warp_smem_floats(int ns, int lroww, int lmat, int Lv) {
-  return align4(ns * stage_floats(lroww, lmat)) + 2 * align4(ns) + align4(2 * (Lv + 1) * 33);
+__host__ __device__ inline int ring_floats(int ns, int lroww, int lmat, int tsize) {
+  return align4((ns * stage_elems(lroww, lmat) * tsize + 3) / 4);
 }
+
+__host__ __device__ inline int warp_smem_floats(int ns, int lroww, int lmat, int Lv, int tsize) {
+  return ring_floats(ns, lroww, lmat, tsize) + 2 * align4(ns) + align4(2 * (Lv + 1) * 33);
+}
+
+template <typename T>
+__device__ __forceinline__ float ldf(T v);
+template <>
+__device__ __forceinline__ float ldf<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float ldf<__half>(__half v) { return __half2float(v); }
+template <typename T>
+__device__ __forceinline__ T stf(float v);
+template <>
+__device__ __forceinline__ float stf<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __half stf<__half>(float v) { return __float2half_rn(v); }
 
 struct WarpSmem {
   float* ring;
@@ -111,33 +145,36 @@ struct ChainSmem {
 // One scanline of one sweep.  Pixels are addressed by their index within the
 // image (pin = y*W + x); the sender of step i is pin0 + i*dpin and its
 // receiver is one dpin further.
+template <typename T>
 struct Chain {
   int n, dir;
   int pin0, dpin;
-  const float* cost;   // batch item n
-  const float* slot_a; // cross-direction message slots read at the sender
-  const float* slot_b;
-  float* slot_out;     // slot written at the receiver (= the incoming chain slot)
+  const T* cost;       // batch item n
+  const T* slot_a;     // cross-direction message slots read at the sender
+  const T* slot_b;
+  T* slot_out;         // slot written at the receiver (= the incoming chain slot)
   int64_t out_off;     // element offset of slot_out within the messages tensor
-  const float* pjump;  // per-pixel pairwise matrices of this direction (pixel variant)
-  int t0, cnt;         // first label of this warp and how many of its labels are < L
+  const T* pjump;      // per-pixel pairwise matrices of this direction (pixel variant)
+  int t0, cnt;         // first label of this warp; labels it copies per row
 };
 
 // Issues the ring stage for step i: the warp's labels [t0, t0+cnt) of the
 // sender's cost and cross-direction messages.
-template <int VARIANT>
-__device__ __forceinline__ void issue_stage(const FwdArgs& a, const Chain& c, const WarpSmem& sm, int lroww,
+template <int VARIANT, typename T>
+__device__ __forceinline__ void issue_stage(const FwdArgs& a, const Chain<T>& c, const WarpSmem& sm, int lroww,
                                             int i, int st, int lane) {
-  float* dst = sm.ring + st * stage_floats(lroww, a.lmat);
-  const int64_t po = static_cast<int64_t>(c.pin0 + i * c.dpin) * a.L + c.t0;
-  const float* src0 = c.cost + po;
-  const float* src1 = c.slot_a + po;
-  const float* src2 = c.slot_b + po;
-  const float* src3 = (VARIANT == BPL_LBP_SEM_PIXEL) ? c.pjump + (po - c.t0) * a.L : nullptr;
+  T* dst = reinterpret_cast<T*>(sm.ring) + st * stage_elems(lroww, a.lmat);
+  const int64_t pin = c.pin0 + i * c.dpin;
+  const int64_t po = pin * a.Ls + c.t0;
+  const T* src0 = c.cost + po;
+  const T* src1 = c.slot_a + po;
+  const T* src2 = c.slot_b + po;
+  const T* src3 = (VARIANT == BPL_LBP_SEM_PIXEL) ? c.pjump + pin * a.L * a.Lm : nullptr;
   if (a.vec4) {
     if (lane == 0) {
-      const uint32_t rb = static_cast<uint32_t>(c.cnt) * 4u;
-      const uint32_t mb = (VARIANT == BPL_LBP_SEM_PIXEL) ? static_cast<uint32_t>(a.L * a.L) * 4u : 0u;
+      const uint32_t rb = static_cast<uint32_t>(c.cnt) * static_cast<uint32_t>(sizeof(T));
+      const uint32_t mb =
+          (VARIANT == BPL_LBP_SEM_PIXEL) ? static_cast<uint32_t>(a.L * a.Lm) * static_cast<uint32_t>(sizeof(T)) : 0u;
       fence_proxy_async();
       mbar_arrive_expect_tx(&sm.bars[st], 3u * rb + mb);
       if (rb > 0) {
@@ -147,14 +184,15 @@ __device__ __forceinline__ void issue_stage(const FwdArgs& a, const Chain& c, co
       }
       if (VARIANT == BPL_LBP_SEM_PIXEL) bulk_g2s(dst + 3 * lroww, src3, mb, &sm.bars[st]);
     }
-  } else {
+  } else if constexpr (sizeof(T) == 4) {
+    // rows not 16-byte sized (float storage only; half rows are padded)
     for (int t = lane; t < c.cnt; t += 32) {
       cp_async4(dst + t, src0 + t);
       cp_async4(dst + lroww + t, src1 + t);
       cp_async4(dst + 2 * lroww + t, src2 + t);
     }
     if (VARIANT == BPL_LBP_SEM_PIXEL)
-      for (int t = lane; t < a.L * a.L; t += 32) cp_async4(dst + 3 * lroww + t, src3 + t);
+      for (int t = lane; t < a.L * a.Lm; t += 32) cp_async4(dst + 3 * lroww + t, src3 + t);
   }
 }
 
@@ -165,7 +203,8 @@ struct TapRegs {
   float w;
 };
 
-__device__ __forceinline__ void load_taps(const FwdArgs& a, const Chain& c, int b, int lane, int nsteps,
+template <typename T>
+__device__ __forceinline__ void load_taps(const FwdArgs& a, const Chain<T>& c, int b, int lane, int nsteps,
                                           TapRegs& r, bool stereo) {
   const int i = 32 * b + lane;
   if (i >= nsteps) return;
@@ -175,7 +214,7 @@ __device__ __forceinline__ void load_taps(const FwdArgs& a, const Chain& c, int 
   r.w = __ldg(a.edge + (static_cast<int64_t>(ne) * 4 + c.dir) * HW + pin);
   if (stereo) {
     const int nj = (a.jb == 1) ? 0 : c.n;
-    const float* base = a.jump + ((static_cast<int64_t>(nj) * 4 + c.dir) * a.Lv) * HW + pin;
+    const float* base = static_cast<const float*>(a.jump) + ((static_cast<int64_t>(nj) * 4 + c.dir) * a.Lv) * HW + pin;
 #pragma unroll
     for (int k = 0; k < 16; ++k)
       if (k < a.Lv) r.t[k] = __ldg(base + static_cast<int64_t>(k) * HW);
@@ -218,8 +257,9 @@ __device__ __forceinline__ void chain_sync(int id) {
 
 // K labels per lane over the chain (label = lane + 32k), KW = K/NW of them
 // owned by each of the chain's NW warps (slots [w*KW, (w+1)*KW)).
-template <int K, int VARIANT, int NW>
+template <int K, int VARIANT, int NW, typename T>
 __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
+  constexpr bool kExact = sizeof(T) == 4;  // float storage: the reference's exact arithmetic
   static_assert(K % NW == 0, "labels must split evenly over the chain's warps");
   static_assert(NW == 1 || VARIANT != BPL_LBP_SEM_PIXEL, "pixel variant runs one warp per chain");
   constexpr int KW = K / NW;
@@ -244,9 +284,9 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
   }
   WarpSmem sm;
   {
-    float* p = smem + cpb * chain_smem_floats(K) + wib * warp_smem_floats(a.ns, lroww, a.lmat, a.Lv);
+    float* p = smem + cpb * chain_smem_floats(K) + wib * warp_smem_floats(a.ns, lroww, a.lmat, a.Lv, sizeof(T));
     sm.ring = p;
-    p += align4(a.ns * stage_floats(lroww, a.lmat));
+    p += ring_floats(a.ns, lroww, a.lmat, sizeof(T));
     sm.bars = reinterpret_cast<uint64_t*>(p);
     p += 2 * align4(a.ns);
     sm.taps = p;
@@ -264,8 +304,9 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
   __syncwarp();
 
   const int64_t HW = static_cast<int64_t>(a.H) * a.W;
-  const int64_t HWL = HW * L;
-  Chain c;
+  const int64_t HWL = HW * a.Ls;  // elements per message slot / cost image
+  const int Ls = a.Ls;
+  Chain<T> c;
   int len;
   {
     const int r = chain_id >> 1;
@@ -290,16 +331,21 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
   const int od = c.dir ^ 1;
   const int sa = (a.phase == 0) ? UP : RIGHT;
   const int sb = (a.phase == 0) ? DOWN : LEFT;
-  c.cost = a.cost + static_cast<int64_t>(c.n) * HWL;
-  c.slot_a = a.msgs + (static_cast<int64_t>(c.n) * 4 + sa) * HWL;
-  c.slot_b = a.msgs + (static_cast<int64_t>(c.n) * 4 + sb) * HWL;
+  c.cost = static_cast<const T*>(a.cost) + static_cast<int64_t>(c.n) * HWL;
+  c.slot_a = static_cast<const T*>(a.msgs) + (static_cast<int64_t>(c.n) * 4 + sa) * HWL;
+  c.slot_b = static_cast<const T*>(a.msgs) + (static_cast<int64_t>(c.n) * 4 + sb) * HWL;
   c.out_off = (static_cast<int64_t>(c.n) * 4 + od) * HWL;
-  c.slot_out = a.msgs + c.out_off;
-  c.pjump = (VARIANT == BPL_LBP_SEM_PIXEL) ? a.jump + static_cast<int64_t>(c.dir) * HWL * L : nullptr;
+  c.slot_out = static_cast<T*>(a.msgs) + c.out_off;
+  c.pjump = (VARIANT == BPL_LBP_SEM_PIXEL)
+                ? static_cast<const T*>(a.jump) + static_cast<int64_t>(c.dir) * HW * L * a.Lm
+                : nullptr;
   c.t0 = 32 * KW * wic;
-  c.cnt = max(0, min(lroww, L - c.t0));
+  // labels copied per row: the warp's labels below Ls (padding included, so
+  // half rows stay 16-byte sized)
+  c.cnt = max(0, min(lroww, Ls - c.t0));
   float* scale_out = a.scale + (static_cast<int64_t>(c.n) * 4 + od) * HW;
-  const float* gjump = (VARIANT == BPL_LBP_SEM_GLOBAL) ? a.jump + static_cast<int64_t>(c.dir) * L * L : nullptr;
+  const float* gjump =
+      (VARIANT == BPL_LBP_SEM_GLOBAL) ? static_cast<const float*>(a.jump) + static_cast<int64_t>(c.dir) * L * L : nullptr;
   const bool stereo = (VARIANT == BPL_LBP_STEREO);
 
   // ring start-up
@@ -309,18 +355,18 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
   }
   __syncwarp();
   for (int i = 0; i < a.ns; ++i) {
-    if (i < nsteps) issue_stage<VARIANT>(a, c, sm, lroww, i, i, lane);
+    if (i < nsteps) issue_stage<VARIANT, T>(a, c, sm, lroww, i, i, lane);
     if (!a.vec4) cp_async_commit();
   }
 
   // incoming chain message at the first sender: the slot the sweep writes
   float chain[KW];
   {
-    const float* src = c.slot_out + static_cast<int64_t>(c.pin0) * L;
+    const T* src = c.slot_out + static_cast<int64_t>(c.pin0) * Ls;
 #pragma unroll
     for (int kk = 0; kk < KW; ++kk) {
       const int t = c.t0 + lane + 32 * kk;
-      chain[kk] = (t < L) ? src[t] : 0.0f;
+      chain[kk] = (t < L) ? ldf<T>(src[t]) : 0.0f;
     }
   }
 
@@ -332,7 +378,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
 
   const int delta = a.delta;
   const int tile_stride = (a.Lv + 1) * 33;
-  const int sf = stage_floats(lroww, a.lmat);
+  const int sf = stage_elems(lroww, a.lmat);
   const float kInf = __int_as_float(0x7f800000);
   bool failed = false;
   int st = 0;
@@ -342,7 +388,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
     const int j = i & 31;
     const int b = i >> 5;
     const float* tile = sm.taps + (b & 1) * tile_stride;
-    const float* stg = sm.ring + st * sf;
+    const T* stg = reinterpret_cast<const T*>(sm.ring) + st * sf;
 
     // wait for stage i (own labels)
     bool ok = true;
@@ -360,9 +406,9 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
     for (int kk = 0; kk < KW; ++kk) {
       const int tl = lane + 32 * kk;  // label within the warp's range
       if (c.t0 + tl < L) {
-        const float cst = stg[tl];
-        const float va = stg[lroww + tl];
-        const float vb = stg[2 * lroww + tl];
+        const float cst = ldf<T>(stg[tl]);
+        const float va = ldf<T>(stg[lroww + tl]);
+        const float vb = ldf<T>(stg[2 * lroww + tl]);
         h[kk] = (a.phase == 0) ? __fadd_rn(__fadd_rn(__fadd_rn(cst, chain[kk]), va), vb)
                                : __fadd_rn(__fadd_rn(__fadd_rn(cst, va), vb), chain[kk]);
       } else {
@@ -391,7 +437,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
     __syncwarp();
     if (VARIANT != BPL_LBP_SEM_PIXEL) {
       // stage consumed: refill it with step i + ns
-      if (i + a.ns < nsteps) issue_stage<VARIANT>(a, c, sm, lroww, i + a.ns, st, lane);
+      if (i + a.ns < nsteps) issue_stage<VARIANT, T>(a, c, sm, lroww, i + a.ns, st, lane);
       if (!a.vec4) cp_async_commit();
     }
     // h of the whole pixel and the partial minima are visible to the chain
@@ -404,6 +450,21 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
     float msg[KW];
     int am[KW];
     float e[KW];
+    // Half storage keeps every message relative to the minimum of h (the
+    // labels near the row's minimum, the ones the beliefs depend on, get
+    // half's finest steps; a log-normalised row sits near -log L, where a
+    // half step is 2^-8).  The row's scale is then the sum of exp of the
+    // stored row, and the log-normalised message is stored - log(scale).
+    float ref = 0.0f;
+    if (!kExact) {
+      ref = pm;
+      if (NW > 1) {
+        ref = cs.red[0];
+#pragma unroll
+        for (int w2 = 1; w2 < NW; ++w2) ref = fminf(ref, cs.red[w2]);
+      }
+    }
+    auto earg = [ref](float x) { return kExact ? x : __fsub_rn(x, ref); };
 
     if (delta >= L) {
       // full minimisation (lbp_min_sum_kernel.cu:88-111): last minimiser wins
@@ -421,7 +482,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
             } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
               f = __ldg(gjump + s * L + t);
             } else {
-              f = stg[3 * lroww + s * L + t];
+              f = ldf<T>(stg[3 * lroww + s * a.Lm + t]);
             }
             const float nm = __fmaf_rn(f, w, cs.hs[s]);
             m = fminf(m, nm);
@@ -435,7 +496,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
       bool eok[KW];
 #pragma unroll
       for (int kk = 0; kk < KW; ++kk) {
-        eok[kk] = crm::exp_fast(msg[kk], e[kk], s_ehi, s_elo);
+        eok[kk] = exp_try<kExact>(earg(msg[kk]), e[kk], s_ehi, s_elo);
         if (c.t0 + lane + 32 * kk >= L) {
           e[kk] = 0.0f;
           eok[kk] = true;
@@ -460,7 +521,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
       } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
         L2 = __ldg(gjump + (L - 1));
       } else {
-        L2 = stg[3 * lroww + (L - 1)];
+        L2 = ldf<T>(stg[3 * lroww + (L - 1)]);
       }
       float wv[KW];
       int wa[KW];
@@ -532,7 +593,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
               } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
                 f = __ldg(gjump + s * L + t);
               } else {
-                f = stg[3 * lroww + s * L + t];
+                f = ldf<T>(stg[3 * lroww + s * a.Lm + t]);
               }
               const float nm = __fmaf_rn(f, w, cs.hs[s]);
               if (nm <= m) {
@@ -564,7 +625,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
       }
       const float msg_g = __fmaf_rn(L2, w, min_h);
       float e_g;
-      if (!crm::exp_fast(msg_g, e_g, s_ehi, s_elo)) e_g = static_cast<float>(exp(static_cast<double>(msg_g)));
+      if (!exp_try<kExact>(earg(msg_g), e_g, s_ehi, s_elo)) e_g = static_cast<float>(exp(static_cast<double>(msg_g)));
       // exact ties of the minimum: the reference tree picks the label
       if (tot > 1) {
         float tv[K];
@@ -589,7 +650,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
         if (__any_sync(FULL, own)) {
           // slot with window winners: their own exp (straight-line code)
           float ex;
-          const bool okx = crm::exp_fast(wv[kk], ex, s_ehi, s_elo);
+          const bool okx = exp_try<kExact>(earg(wv[kk]), ex, s_ehi, s_elo);
           e[kk] = own ? ex : e[kk];
           all_ok = all_ok && (okx || !own);
         }
@@ -606,7 +667,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
 
     if (VARIANT == BPL_LBP_SEM_PIXEL) {
       __syncwarp();
-      if (i + a.ns < nsteps) issue_stage<VARIANT>(a, c, sm, lroww, i + a.ns, st, lane);
+      if (i + a.ns < nsteps) issue_stage<VARIANT, T>(a, c, sm, lroww, i + a.ns, st, lane);
       if (!a.vec4) cp_async_commit();
     }
 
@@ -626,17 +687,19 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
       for (int k = 0; k < K; ++k) ev[k] = cs.erow[lane + 32 * k];
       sum = tree_sum<K>(ev, L, lane);
     }
-    const float lse = norm_log(sum);
+    // subtracted from every label: log of the sum (the reference's
+    // normalisation) for float storage, the minimum of h for half storage
+    const float lse = kExact ? norm_log(sum) : ref;
 
     // write the message at the receiver
     const int pq = pin + c.dpin;
-    const int64_t qo = static_cast<int64_t>(pq) * L;
-    float* dstm = c.slot_out + qo;
+    const int64_t qo = static_cast<int64_t>(pq) * Ls;
+    T* dstm = c.slot_out + qo;
 #pragma unroll
     for (int kk = 0; kk < KW; ++kk) {
       const int t = c.t0 + lane + 32 * kk;
-      const float o = __fsub_rn(msg[kk], lse);
-      chain[kk] = o;
+      const T o = stf<T>(__fsub_rn(msg[kk], lse));
+      chain[kk] = ldf<T>(o);  // the stored value, so the chain matches memory
       if (t < L) {
         dstm[t] = o;
         const int64_t ao = c.out_off + qo + t;
@@ -674,15 +737,15 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
 }
 
 // Host-side launch of one phase for one (K, variant, NW) instantiation.
-template <int K, int V, int NW>
+template <int K, int V, int NW, typename T>
 int launch_phase(const FwdArgs& a, cudaStream_t stream) {
   const int lroww = 32 * (K / NW);
   const size_t per_chain = 4 * (static_cast<size_t>(chain_smem_floats(K)) +
-                                static_cast<size_t>(NW) * warp_smem_floats(a.ns, lroww, a.lmat, a.Lv));
+                                static_cast<size_t>(NW) * warp_smem_floats(a.ns, lroww, a.lmat, a.Lv, sizeof(T)));
   // chains per block: up to 4 warps while the block fits in 200 KB
   const int cpb = std::max(1, std::min(4 / NW, static_cast<int>((200 * 1024) / per_chain)));
   const size_t smem = per_chain * cpb;
-  auto kern = lbp_forward_kernel<K, V, NW>;
+  auto kern = lbp_forward_kernel<K, V, NW, T>;
   if (smem > 48 * 1024) {
     if (static_cast<int>(smem) > max_smem_optin())
       return set_error(BPL_ERR_UNSUPPORTED, "lbp_forward: shared memory %zu exceeds device limit", smem);
@@ -702,58 +765,58 @@ inline bool split_chains(int nchains) { return nchains < kSplitChainsPerSm * sm_
 
 // K: register slots per lane (K * 32 >= L).  KS, NS: the instantiation and
 // warp count used when a phase's scanlines are split.
-template <int K, int V, int KS, int NS>
+template <int K, int V, int KS, int NS, typename T>
 int launch_k(const FwdArgs& a0, cudaStream_t stream) {
   FwdArgs a = a0;
   for (int phase = 0; phase < 2; ++phase) {
     a.phase = phase;
     a.nchains = 2 * a.B * (phase == 0 ? a.H : a.W);
     int st;
-    if (NS > 1 && split_chains(a.nchains)) st = launch_phase<KS, V, NS>(a, stream);
-    else st = launch_phase<K, V, 1>(a, stream);
+    if (NS > 1 && split_chains(a.nchains)) st = launch_phase<KS, V, NS, T>(a, stream);
+    else st = launch_phase<K, V, 1, T>(a, stream);
     if (st != BPL_OK) return st;
   }
   return BPL_OK;
 }
 
-template <int V>
+template <int V, typename T = float>
 int dispatch_k(const FwdArgs& a, cudaStream_t s) {
   const int k = (a.L + 31) / 32;
   if constexpr (V != BPL_LBP_STEREO) {
     // semantic variants: one warp per scanline
     if constexpr (V == BPL_LBP_SEM_PIXEL) {
       // per-pixel L x L matrices: L <= 96 (checked at the entry point)
-      if (k == 1) return launch_k<1, V, 1, 1>(a, s);
-      if (k == 2) return launch_k<2, V, 2, 1>(a, s);
-      return launch_k<3, V, 3, 1>(a, s);
+      if (k == 1) return launch_k<1, V, 1, 1, T>(a, s);
+      if (k == 2) return launch_k<2, V, 2, 1, T>(a, s);
+      return launch_k<3, V, 3, 1, T>(a, s);
     }
     switch (k) {
-      case 1: return launch_k<1, V, 1, 1>(a, s);
-      case 2: return launch_k<2, V, 2, 1>(a, s);
-      case 3: return launch_k<3, V, 3, 1>(a, s);
-      case 4: return launch_k<4, V, 4, 1>(a, s);
+      case 1: return launch_k<1, V, 1, 1, T>(a, s);
+      case 2: return launch_k<2, V, 2, 1, T>(a, s);
+      case 3: return launch_k<3, V, 3, 1, T>(a, s);
+      case 4: return launch_k<4, V, 4, 1, T>(a, s);
       default:
-        if (k <= 8) return launch_k<8, V, 8, 1>(a, s);
-        if (k <= 16) return launch_k<16, V, 16, 1>(a, s);
-        return launch_k<32, V, 32, 1>(a, s);
+        if (k <= 8) return launch_k<8, V, 8, 1, T>(a, s);
+        if (k <= 16) return launch_k<16, V, 16, 1, T>(a, s);
+        return launch_k<32, V, 32, 1, T>(a, s);
     }
   } else {
     // (the split-scanline instantiations KS/NS are enabled together with
     // kSplitChainsPerSm; with it at 0 every phase runs one warp per scanline)
     switch (k) {
-      case 1: return launch_k<1, V, 1, 1>(a, s);
-      case 2: return launch_k<2, V, 2, 1>(a, s);
-      case 3: return launch_k<3, V, 3, 1>(a, s);
-      case 4: return launch_k<4, V, 4, 1>(a, s);
-      case 5: return launch_k<5, V, 5, 1>(a, s);
-      case 6: return launch_k<6, V, 6, 1>(a, s);
-      case 7: return launch_k<7, V, 7, 1>(a, s);
-      case 8: return launch_k<8, V, 8, 1>(a, s);
+      case 1: return launch_k<1, V, 1, 1, T>(a, s);
+      case 2: return launch_k<2, V, 2, 1, T>(a, s);
+      case 3: return launch_k<3, V, 3, 1, T>(a, s);
+      case 4: return launch_k<4, V, 4, 1, T>(a, s);
+      case 5: return launch_k<5, V, 5, 1, T>(a, s);
+      case 6: return launch_k<6, V, 6, 1, T>(a, s);
+      case 7: return launch_k<7, V, 7, 1, T>(a, s);
+      case 8: return launch_k<8, V, 8, 1, T>(a, s);
       default:
-        if (k <= 12) return launch_k<12, V, 12, 1>(a, s);
-        if (k <= 16) return launch_k<16, V, 16, 1>(a, s);
-        if (k <= 24) return launch_k<24, V, 24, 1>(a, s);
-        return launch_k<32, V, 32, 1>(a, s);
+        if (k <= 12) return launch_k<12, V, 12, 1, T>(a, s);
+        if (k <= 16) return launch_k<16, V, 16, 1, T>(a, s);
+        if (k <= 24) return launch_k<24, V, 24, 1, T>(a, s);
+        return launch_k<32, V, 32, 1, T>(a, s);
     }
   }
 }
@@ -761,5 +824,7 @@ int dispatch_k(const FwdArgs& a, cudaStream_t s) {
 int lbp_forward_stereo(const FwdArgs& a, cudaStream_t s);
 int lbp_forward_sem_global(const FwdArgs& a, cudaStream_t s);
 int lbp_forward_sem_pixel(const FwdArgs& a, cudaStream_t s);
+int lbp_forward_stereo_f16(const FwdArgs& a, cudaStream_t s);
+int lbp_forward_sem_pixel_f16(const FwdArgs& a, cudaStream_t s);
 
 }  // namespace bpl

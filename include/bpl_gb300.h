@@ -85,6 +85,27 @@ int bpl_lbp_forward(int variant, const float* cost, const float* jump, const flo
                     float* messages, void* argmin, int argmin_kind, float* scale, int B, int H,
                     int W, int L, int Lv, int jump_batch, int edge_batch, int delta, void* stream);
 
+/*
+ * LBP forward with FP16 storage: cost and messages (and the pixel-pairwise
+ * matrices) stored as IEEE half, all arithmetic in FP32, the normalisation's
+ * exp by the hardware approximation.  No counterpart in the reference
+ * (which is FP32 only); same sweeps and tie rules as bpl_lbp_forward.
+ * Stored messages are referenced to the minimum of h instead of
+ * log-normalised: row = m_raw - min_s h(s), scale = sum_t exp(row[t]), so
+ * the reference's normalised message is row - log(scale).  Beliefs built
+ * from them differ from the reference's by a constant per pixel (their
+ * argmin and softmin are unchanged), and half's finest steps fall on the
+ * labels near the row's minimum.
+ * Layout: the label axis has stride Lp = L rounded up to 8 (16-byte rows):
+ *   cost (B,H,W,Lp) half, messages (B,4,H,W,Lp) half, argmin (B,4,H,W,Lp),
+ *   pixel-pairwise jump (4,H,W,L,Lp) half; stereo jump taps, edge and scale
+ *   stay float.  Labels L..Lp-1 are ignored on input and not written.
+ * Variants: BPL_LBP_STEREO and BPL_LBP_SEM_PIXEL.
+ */
+int bpl_lbp_forward_f16(int variant, const void* cost, const void* jump, const float* edge,
+                        void* messages, void* argmin, int argmin_kind, float* scale, int B, int H,
+                        int W, int L, int Lv, int jump_batch, int edge_batch, int delta, void* stream);
+
 /* Bytes of device workspace bpl_lbp_backward needs: B*2*H*W*L floats (the
  * vertical sweeps' chain gradients that the horizontal sweeps read; the
  * reference allocates the same as saved_prev_grad_msg,
@@ -123,6 +144,22 @@ int bpl_lbp_backward(int variant, const float* jump, const float* edge, const fl
 /* Disparity count D of the SAD volume: (int)((max_disp - min_disp + 1) / step)
  * (ops/sad/src/stereo_sad_kernel.cu:122); -1 for a non-positive step. */
 int bpl_sad_volume_depth(int min_disp, int max_disp, float step);
+
+/*
+ * Reference adjoint for FP16-stored messages (the layout of
+ * bpl_lbp_forward_f16: label axis padded to Lp = L rounded up to 8).  No
+ * counterpart in the reference.  in_grad and messages (B,4,H,W,Lp) half,
+ * messages and scale as bpl_lbp_forward_f16 wrote them (min-referenced rows);
+ * argmin (B,4,H,W,Lp); grad_cost (B,H,W,Lp) float (labels >= L are zero);
+ * grad_jump / grad_edge as bpl_lbp_backward (float, unpadded).  workspace:
+ * bpl_lbp_backward_workspace_size(B, H, W, Lp) bytes.  Variants
+ * BPL_LBP_STEREO and BPL_LBP_SEM_PIXEL.
+ */
+int bpl_lbp_backward_f16(int variant, const float* jump, const float* edge, const void* in_grad,
+                         const void* messages, const void* argmin, int argmin_kind, const float* scale,
+                         float* grad_cost, float* grad_jump, float* grad_edge, void* workspace,
+                         size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
+                         int edge_batch, void* stream);
 
 /*
  * Stereo SAD cost volume.  Replaces cuda::stereo_sad_forward
