@@ -106,6 +106,17 @@ __device__ __forceinline__ float tree_sum(float (&v)[K], int L, int lane) {
 
 // Plain warp sum (any order) for the adjoint kernels, which have no bitwise
 // parity target (the reference uses float atomics).
+// Order-preserving map of floats onto unsigned integers (-0 below +0, NaN
+// above +inf), so that a warp minimum is one redux.sync instruction.
+__device__ __forceinline__ unsigned f2ord(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+__device__ __forceinline__ float warp_min_redux(float v) { return ord2f(__reduce_min_sync(0xffffffffu, f2ord(v))); }
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);

@@ -65,7 +65,10 @@ int lbp_forward_impl(int storage, int variant, const void* cost, const void* jum
     a.lmat = (variant == BPL_LBP_SEM_PIXEL) ? L * a.Lm : 0;
     a.vec4 = 1;
   }
-  a.ns = a.vec4 ? 4 : kRingCpAsync;
+  // shared-memory ring (pixel variant only): 4 steps in flight, one step
+  // per mbarrier group; the other variants prefetch rows into registers
+  a.ns = (variant == BPL_LBP_SEM_PIXEL) ? (a.vec4 ? 4 : kRingCpAsync) : 0;
+  a.sps = 1;
   cudaStream_t s = as_stream(stream);
   if (storage == 1) return (variant == BPL_LBP_STEREO) ? lbp_forward_stereo_f16(a, s) : lbp_forward_sem_pixel_f16(a, s);
   switch (variant) {

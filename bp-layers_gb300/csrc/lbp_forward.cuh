@@ -47,6 +47,8 @@ constexpr int kHsPad = 4;
 // scanline's labels over several warps (0: never; the split pays only when
 // the per-label work dominates the per-step reductions).
 constexpr int kSplitChainsPerSm = 0;
+// scanlines per SM above which a phase runs the high-occupancy instantiation
+constexpr int kHiOccChainsPerSm = 8;
 
 // Storage type T of cost, messages (and the pixel-pairwise matrices): float
 // (reference layout, bit-exact) or __half (FP16 storage, FP32 arithmetic).
@@ -65,7 +67,8 @@ struct FwdArgs {
   int argmin_kind;
   int phase;  // 0: RIGHT+LEFT over rows, 1: DOWN+UP over columns
   int nchains;
-  int ns;     // ring depth
+  int ns;     // ring depth (steps)
+  int sps;    // steps per ring group (one mbarrier per group)
   int lrow;   // unused
   int lmat;   // elements of the per-pixel pairwise matrix in a stage (pixel variant), else 0
   int vec4;   // rows are 16-byte sized: use bulk copies
@@ -101,11 +104,15 @@ __device__ __forceinline__ float norm_log(float sum) {
 //   per warp:  ring ns stages x 3 rows x lroww floats (cost and the two
 //              cross-direction messages of the warp's own labels [+ the
 //              pixel's L x L pairwise matrix, pixel variant]), ns mbarriers,
-//              taps tile 2 x (Lv+1) x 33 floats.
+//              taps tile 2 x (Lv+3) x 33 floats.
 __host__ __device__ inline int align4(int v) { return (v + 3) & ~3; }
 
 // elements of T per ring stage
 __host__ __device__ inline int stage_elems(int lrow, int lmat) { return 3 * lrow + lmat; }
+
+// rows of a warp's tap tile: Lv taps, the edge weight, the window class of
+// the sender (two rows)
+__host__ __device__ inline int tap_tile_rows(int Lv) { return Lv + 3; }
 
 __host__ __device__ inline int chain_smem_floats(int K) { return align4(32 * K + 2 * kHsPad) + 32 * K + 16; }
 
@@ -114,7 +121,7 @@ __host__ __device__ inline int ring_floats(int ns, int lroww, int lmat, int tsiz
 }
 
 __host__ __device__ inline int warp_smem_floats(int ns, int lroww, int lmat, int Lv, int tsize) {
-  return ring_floats(ns, lroww, lmat, tsize) + 2 * align4(ns) + align4(2 * (Lv + 1) * 33);
+  return ring_floats(ns, lroww, lmat, tsize) + 2 * align4(ns) + align4(2 * tap_tile_rows(Lv) * 33);
 }
 
 template <typename T>
@@ -158,11 +165,12 @@ struct Chain {
   int t0, cnt;         // first label of this warp; labels it copies per row
 };
 
-// Issues the ring stage for step i: the warp's labels [t0, t0+cnt) of the
-// sender's cost and cross-direction messages.
+// Issues ring slot `st` for step i: the warp's labels [t0, t0+cnt) of the
+// sender's cost and cross-direction messages (+ the pixel's pairwise matrix,
+// pixel variant).  Bulk copies complete on `bar`; the caller arms it.
 template <int VARIANT, typename T>
-__device__ __forceinline__ void issue_stage(const FwdArgs& a, const Chain<T>& c, const WarpSmem& sm, int lroww,
-                                            int i, int st, int lane) {
+__device__ __forceinline__ void issue_slot(const FwdArgs& a, const Chain<T>& c, const WarpSmem& sm, int lroww,
+                                           int i, int st, uint64_t* bar, int lane) {
   T* dst = reinterpret_cast<T*>(sm.ring) + st * stage_elems(lroww, a.lmat);
   const int64_t pin = c.pin0 + i * c.dpin;
   const int64_t po = pin * a.Ls + c.t0;
@@ -173,16 +181,13 @@ __device__ __forceinline__ void issue_stage(const FwdArgs& a, const Chain<T>& c,
   if (a.vec4) {
     if (lane == 0) {
       const uint32_t rb = static_cast<uint32_t>(c.cnt) * static_cast<uint32_t>(sizeof(T));
-      const uint32_t mb =
-          (VARIANT == BPL_LBP_SEM_PIXEL) ? static_cast<uint32_t>(a.L * a.Lm) * static_cast<uint32_t>(sizeof(T)) : 0u;
-      fence_proxy_async();
-      mbar_arrive_expect_tx(&sm.bars[st], 3u * rb + mb);
       if (rb > 0) {
-        bulk_g2s(dst, src0, rb, &sm.bars[st]);
-        bulk_g2s(dst + lroww, src1, rb, &sm.bars[st]);
-        bulk_g2s(dst + 2 * lroww, src2, rb, &sm.bars[st]);
+        bulk_g2s(dst, src0, rb, bar);
+        bulk_g2s(dst + lroww, src1, rb, bar);
+        bulk_g2s(dst + 2 * lroww, src2, rb, bar);
       }
-      if (VARIANT == BPL_LBP_SEM_PIXEL) bulk_g2s(dst + 3 * lroww, src3, mb, &sm.bars[st]);
+      if (VARIANT == BPL_LBP_SEM_PIXEL)
+        bulk_g2s(dst + 3 * lroww, src3, static_cast<uint32_t>(a.L * a.Lm) * static_cast<uint32_t>(sizeof(T)), bar);
     }
   } else if constexpr (sizeof(T) == 4) {
     // rows not 16-byte sized (float storage only; half rows are padded)
@@ -194,6 +199,26 @@ __device__ __forceinline__ void issue_stage(const FwdArgs& a, const Chain<T>& c,
     if (VARIANT == BPL_LBP_SEM_PIXEL)
       for (int t = lane; t < a.L * a.Lm; t += 32) cp_async4(dst + 3 * lroww + t, src3 + t);
   }
+}
+
+// Issues ring group g (slots [g*sps, (g+1)*sps)) for steps [i0, i0 + sps)
+// below nsteps: one mbarrier armed with the bytes of all of them.  With
+// cp.async rows (sps = 1) the caller commits one group per step.
+template <int VARIANT, typename T>
+__device__ __forceinline__ void issue_group(const FwdArgs& a, const Chain<T>& c, const WarpSmem& sm, int lroww,
+                                            int i0, int g, int nsteps, int lane) {
+  const int n = min(a.sps, nsteps - i0);
+  if (n <= 0) return;
+  uint64_t* bar = &sm.bars[g];
+  if (a.vec4 && lane == 0) {
+    const uint32_t rb = static_cast<uint32_t>(c.cnt) * static_cast<uint32_t>(sizeof(T));
+    const uint32_t mb =
+        (VARIANT == BPL_LBP_SEM_PIXEL) ? static_cast<uint32_t>(a.L * a.Lm) * static_cast<uint32_t>(sizeof(T)) : 0u;
+    // the slots were last read through the generic proxy
+    fence_proxy_async();
+    mbar_arrive_expect_tx(bar, static_cast<uint32_t>(n) * (3u * rb + mb));
+  }
+  for (int k = 0; k < n; ++k) issue_slot<VARIANT, T>(a, c, sm, lroww, i0 + k, g * a.sps + k, bar, lane);
 }
 
 // Stereo taps + edge weight for the 32 pixels of block b: lane j loads the
@@ -221,14 +246,59 @@ __device__ __forceinline__ void load_taps(const FwdArgs& a, const Chain<T>& c, i
   }
 }
 
+// Window classes of a sender's zero-offset truncation window (stereo, delta
+// <= kFastDelta).  A window term fmaf(f, w, h(s)) whose tap has f*w >= L2*w
+// is >= the global candidate fmaf(L2, w, min h) (h(s) >= min h, rounding is
+// monotone): it can tie the candidate but never beat it ("tie-only"
+// offset).  When the offsets that can beat it are exactly |jd| <= R, the
+// message needs only those 2R+1 terms plus an exact check of the tie-only
+// offsets against the few senders that can reach the candidate there.
+//   code 0: no fast form (offset, delta or tap pattern)
+//   code 1..4: R = code - 2 (R = -1: no offset beats the candidate)
+//   bit 8: the window holds tie-only offsets; the tile row Lv+1 then holds
+//          the tie-only tap of smallest product with w
+constexpr int kWinGeneric = 0;
+constexpr int kWinHasTieOnly = 0x100;
+
 __device__ __forceinline__ void store_taps(const FwdArgs& a, float* tile, int lane, const TapRegs& r,
                                            bool stereo) {
-  // tile layout: [Lv+1][33]; row Lv holds the edge weight
+  // tile layout: [Lv+3][33]; rows 0..Lv-1 taps, row Lv the edge weight,
+  // row Lv+1 the smallest-product tie-only tap, row Lv+2 the window code
   tile[a.Lv * 33 + lane] = r.w;
   if (stereo) {
 #pragma unroll
     for (int k = 0; k < 16; ++k)
       if (k < a.Lv) tile[k * 33 + lane] = r.t[k];
+    // each lane classifies its own column (no other lane's values are read)
+    const float w = r.w;
+    const float L2 = tile[(a.Lv - 1) * 33 + lane];
+    int code = kWinGeneric;
+    float fnr = 0.0f;
+    if (tile[lane] == 0.0f && a.delta <= kFastDelta) {
+      int R = -1;
+      bool ok = true, seen_tie = false, have_tie = false;
+      for (int q = 0; q <= a.delta; ++q) {
+        const float fp = tile[max(1, min(a.Lv - 1, a.Lv / 2 - q)) * 33 + lane];  // jd = +q
+        const float fm = tile[max(1, min(a.Lv - 1, a.Lv / 2 + q)) * 33 + lane];  // jd = -q
+        const bool tp = (w > 0.0f) ? (fp >= L2) : ((w < 0.0f) ? (fp <= L2) : true);
+        const bool tm = (w > 0.0f) ? (fm >= L2) : ((w < 0.0f) ? (fm <= L2) : true);
+        if (!tp && !tm) {
+          if (seen_tie) ok = false;
+          R = q;
+        } else if (tp && tm) {
+          seen_tie = true;
+          // tie-only tap of smallest product f*w
+          const float f = (w >= 0.0f) ? fminf(fp, fm) : fmaxf(fp, fm);
+          fnr = !have_tie ? f : ((w >= 0.0f) ? fminf(fnr, f) : fmaxf(fnr, f));
+          have_tie = true;
+        } else {
+          ok = false;
+        }
+      }
+      if (ok && R <= 2) code = (R + 2) | (have_tie ? kWinHasTieOnly : 0);
+    }
+    tile[(a.Lv + 1) * 33 + lane] = fnr;
+    tile[(a.Lv + 2) * 33 + lane] = __int_as_float(code);
   }
 }
 
@@ -257,8 +327,11 @@ __device__ __forceinline__ void chain_sync(int id) {
 
 // K labels per lane over the chain (label = lane + 32k), KW = K/NW of them
 // owned by each of the chain's NW warps (slots [w*KW, (w+1)*KW)).
-template <int K, int VARIANT, int NW, typename T>
-__global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
+// OCC: blocks per SM the register allocation must allow (1 for the
+// latency-bound phase with few scanlines, more where scanlines outnumber
+// the warps one wave holds).
+template <int K, int VARIANT, int NW, typename T, int OCC>
+__global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
   constexpr bool kExact = sizeof(T) == 4;  // float storage: the reference's exact arithmetic
   static_assert(K % NW == 0, "labels must split evenly over the chain's warps");
   static_assert(NW == 1 || VARIANT != BPL_LBP_SEM_PIXEL, "pixel variant runs one warp per chain");
@@ -348,15 +421,35 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
       (VARIANT == BPL_LBP_SEM_GLOBAL) ? static_cast<const float*>(a.jump) + static_cast<int64_t>(c.dir) * L * L : nullptr;
   const bool stereo = (VARIANT == BPL_LBP_STEREO);
 
-  // ring start-up
-  if (a.vec4 && lane == 0) {
-    for (int s = 0; s < a.ns; ++s) mbar_init(&sm.bars[s], 1);
+  // Pixel variant: a shared-memory ring of the steps' rows and L x L
+  // matrices (groups of sps steps, one mbarrier each).  Other variants: the
+  // next step's own rows are prefetched into registers (coalesced loads of
+  // data no sweep of this phase writes), one step ahead.
+  constexpr bool kRing = (VARIANT == BPL_LBP_SEM_PIXEL);
+  const int G = kRing ? a.sps : 1;
+  T ncst[KW], nva[KW], nvb[KW];  // raw: converted when used, so the loads do not stall here
+  auto prefetch = [&](int i) {
+    const int64_t po = static_cast<int64_t>(c.pin0 + i * c.dpin) * Ls;
+#pragma unroll
+    for (int kk = 0; kk < KW; ++kk) {
+      const int t = c.t0 + lane + 32 * kk;
+      const int64_t o = po + ((t < L) ? t : 0);  // labels >= L read label 0 (ignored)
+      ncst[kk] = __ldg(c.cost + o);
+      nva[kk] = __ldg(c.slot_a + o);
+      nvb[kk] = __ldg(c.slot_b + o);
+    }
+  };
+  if (!kRing) prefetch(0);
+  if (kRing && a.vec4 && lane == 0) {
+    for (int g = 0; g < a.ns / G; ++g) mbar_init(&sm.bars[g], 1);
     fence_mbar_init();
   }
   __syncwarp();
-  for (int i = 0; i < a.ns; ++i) {
-    if (i < nsteps) issue_stage<VARIANT, T>(a, c, sm, lroww, i, i, lane);
-    if (!a.vec4) cp_async_commit();
+  if (kRing) {
+    for (int i0 = 0; i0 < a.ns; i0 += G) {
+      issue_group<VARIANT, T>(a, c, sm, lroww, i0, i0 / G, nsteps, lane);
+      if (!a.vec4) cp_async_commit();
+    }
   }
 
   // incoming chain message at the first sender: the slot the sweep writes
@@ -377,7 +470,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
   __syncwarp();
 
   const int delta = a.delta;
-  const int tile_stride = (a.Lv + 1) * 33;
+  const int tile_stride = tap_tile_rows(a.Lv) * 33;
   const int sf = stage_elems(lroww, a.lmat);
   const float kInf = __int_as_float(0x7f800000);
   bool failed = false;
@@ -390,58 +483,64 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
     const float* tile = sm.taps + (b & 1) * tile_stride;
     const T* stg = reinterpret_cast<const T*>(sm.ring) + st * sf;
 
-    // wait for stage i (own labels)
+    // wait for the ring group of step i (own labels) at its first step
+    const int grp = st / G;
     bool ok = true;
-    if (a.vec4) {
-      ok = mbar_wait_bounded(&sm.bars[st], par);
-    } else {
-      cp_async_wait<kRingCpAsync - 1>();  // groups 0..i have landed
+    if (kRing && st == grp * G) {
+      if (a.vec4) {
+        ok = mbar_wait_bounded(&sm.bars[grp], (par >> grp) & 1u);
+        par ^= 1u << grp;
+      } else {
+        cp_async_wait<kRingCpAsync - 1>();  // groups 0..i have landed
+      }
+      __syncwarp();
     }
-    __syncwarp();
 
     // h = cost + incoming messages except the chain direction's own slot,
     // added in the reference order RIGHT, LEFT, UP, DOWN.
     float h[KW];
 #pragma unroll
     for (int kk = 0; kk < KW; ++kk) {
+      // branch-free: the ring rows are lroww long; labels >= L read padding
+      // and get +inf (never a minimum)
       const int tl = lane + 32 * kk;  // label within the warp's range
-      if (c.t0 + tl < L) {
-        const float cst = ldf<T>(stg[tl]);
-        const float va = ldf<T>(stg[lroww + tl]);
-        const float vb = ldf<T>(stg[2 * lroww + tl]);
-        h[kk] = (a.phase == 0) ? __fadd_rn(__fadd_rn(__fadd_rn(cst, chain[kk]), va), vb)
-                               : __fadd_rn(__fadd_rn(__fadd_rn(cst, va), vb), chain[kk]);
-      } else {
-        h[kk] = kInf;  // never a minimum
-      }
+      const float cst = ldf<T>(kRing ? stg[tl] : ncst[kk]);
+      const float va = ldf<T>(kRing ? stg[lroww + tl] : nva[kk]);
+      const float vb = ldf<T>(kRing ? stg[2 * lroww + tl] : nvb[kk]);
+      const float hv = (a.phase == 0) ? __fadd_rn(__fadd_rn(__fadd_rn(cst, chain[kk]), va), vb)
+                                      : __fadd_rn(__fadd_rn(__fadd_rn(cst, va), vb), chain[kk]);
+      h[kk] = (c.t0 + tl < L) ? hv : kInf;
       cs.hs[c.t0 + tl] = h[kk];
     }
-    // partial minimum over the warp's labels, with its tie count and label
+    // partial minimum over the warp's labels (one redux), with its tie count
+    // and, when the minimum is unique, its label
     float pm = h[0];
 #pragma unroll
     for (int kk = 1; kk < KW; ++kk) pm = fminf(pm, h[kk]);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) pm = fminf(pm, __shfl_xor_sync(FULL, pm, o));
-    int pcnt = 0, plab = 0;
+    pm = warp_min_redux(pm);
+    int lcnt = 0, llab = 0;
 #pragma unroll
     for (int kk = 0; kk < KW; ++kk) {
-      const unsigned m = __ballot_sync(FULL, h[kk] == pm);
-      pcnt += __popc(m);
-      if (m) plab = c.t0 + 32 * kk + __ffs(m) - 1;
+      const bool eq = h[kk] == pm;
+      lcnt += eq ? 1 : 0;
+      llab = eq ? c.t0 + lane + 32 * kk : llab;
     }
+    const int pcnt = __reduce_add_sync(FULL, lcnt);
+    const int plab = __reduce_max_sync(FULL, llab);
     if (NW > 1 && lane == 0) {
       cs.red[wic] = pm;
       reinterpret_cast<int*>(cs.red)[4 + wic] = pcnt;
       reinterpret_cast<int*>(cs.red)[8 + wic] = plab;
     }
     __syncwarp();
-    if (VARIANT != BPL_LBP_SEM_PIXEL) {
-      // stage consumed: refill it with step i + ns
-      if (i + a.ns < nsteps) issue_stage<VARIANT, T>(a, c, sm, lroww, i + a.ns, st, lane);
-      if (!a.vec4) cp_async_commit();
-    }
+    if (!kRing && i + 1 < nsteps) prefetch(i + 1);
     // h of the whole pixel and the partial minima are visible to the chain
-    if (!chain_sync_and<NW>(bar_id, ok)) {
+    if (NW == 1) {
+      if (!__all_sync(FULL, ok)) {
+        failed = true;
+        break;
+      }
+    } else if (!chain_sync_and<NW>(bar_id, ok)) {
       failed = true;
       break;
     }
@@ -513,7 +612,11 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
       // starts from the global candidate fmaf(L2, w, min h) and scans the
       // window in increasing label order with `<=`; that equals taking the
       // window's own minimum (last label on ties) when it is <= the global
-      // candidate, so the window scan needs no global minimum and runs first.
+      // candidate.  A sender s can only reach the candidate if
+      // fmaf(f*, w, h(s)) <= fmaf(L2, w, min h), f* the tap of smallest
+      // product (rounding is monotone), so with a zero offset only the slots
+      // whose windows hold such a sender are scanned; every other label takes
+      // the candidate, its argmin and its exp.
       float L2, off = 0.0f;
       if (stereo) {
         L2 = tile[(a.Lv - 1) * 33 + j];
@@ -523,25 +626,162 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
       } else {
         L2 = ldf<T>(stg[3 * lroww + (L - 1)]);
       }
-      float wv[KW];
-      int wa[KW];
-      if (stereo && delta <= kFastDelta && off == 0.0f) {
-        // Zero offset: the window is [t-delta, t+delta] clipped to [0, L),
-        // and the tap of sender s = t + jd is clamp(Lv/2 - jd, 1, Lv-1), the
-        // same for every label.  hs holds +inf outside [0, L), which never
-        // wins against the finite global candidate, in place of the clipping.
-        float fj[2 * kFastDelta + 1];
+      // The global candidate needs only the minimum value of h, which any
+      // reduction order gives exactly.
+      float min_h = pm;
+      int argmin_h = plab, tot = pcnt;
+      if (NW > 1) {
+        min_h = cs.red[0];
 #pragma unroll
-        for (int q = 0; q <= 2 * kFastDelta; ++q) {
-          const int ti = max(1, min(a.Lv - 1, a.Lv / 2 - (q - kFastDelta)));
-          fj[q] = tile[ti * 33 + j];
+        for (int w2 = 1; w2 < NW; ++w2) min_h = fminf(min_h, cs.red[w2]);
+        tot = 0;
+#pragma unroll
+        for (int w2 = 0; w2 < NW; ++w2)
+          if (cs.red[w2] == min_h) {
+            tot += reinterpret_cast<const int*>(cs.red)[4 + w2];
+            argmin_h = reinterpret_cast<const int*>(cs.red)[8 + w2];
+          }
+      }
+      // exact ties of the minimum: the reference tree picks the label (and,
+      // between -0 and +0, the value)
+      if (tot > 1) {
+        float tv[K];
+        int tl[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          tv[k] = cs.hs[lane + 32 * k];
+          tl[k] = lane + 32 * k;
         }
-        if (delta == 3) {
+        float mv;
+        tree_argmin<K>(tv, tl, L, lane, mv, argmin_h);
+        min_h = cs.hs[argmin_h];
+      }
+      const float msg_g = __fmaf_rn(L2, w, min_h);
+
+      // Fast form (one warp per scanline, stereo zero-offset windows whose
+      // beating offsets are |jd| <= R): the 2R+1 terms for every label, and
+      // the tie-only offsets checked against the one sender s1 that can reach
+      // the candidate there (fmaf(f_tie, w, h(s1)) <= candidate for the
+      // smallest-product tie-only tap); with several such senders, or no
+      // fast form, every window term is scanned.
+      int R = -2;
+      int s1 = -1;
+      if (NW == 1 && stereo) {
+        const int wcode = __float_as_int(tile[(a.Lv + 2) * 33 + j]);
+        if ((wcode & 0xff) != kWinGeneric) {
+          R = (wcode & 0xff) - 2;
+          if (wcode & kWinHasTieOnly) {
+            const float fnr = tile[(a.Lv + 1) * 33 + j];
+            int lc = 0, ll = -1;
+#pragma unroll
+            for (int kk = 0; kk < KW; ++kk) {
+              const bool nr = __fmaf_rn(fnr, w, h[kk]) <= msg_g;  // +inf (no label) never is
+              lc += nr ? 1 : 0;
+              ll = nr ? c.t0 + lane + 32 * kk : ll;
+            }
+            const int nn = __reduce_add_sync(FULL, lc);
+            if (nn > 1) R = -2;
+            else if (nn == 1) s1 = __reduce_max_sync(FULL, ll);
+          }
+        }
+      }
+      bool own[KW];
+      if (R >= -1) {
+        // the 2R+1 beating terms of every label, straight-line per path
+        // (uniform branches outside the label loops keep the slots
+        // independent); hs holds +inf outside [0, L)
+        float mw[KW];
+        int aw[KW];
+        const int c0 = a.Lv / 2;
+        if (R == 1) {
+          const float fm1 = tile[min(a.Lv - 1, c0 + 1) * 33 + j];  // sender t-1
+          const float f00 = tile[c0 * 33 + j];                     // sender t
+          const float fp1 = tile[max(1, c0 - 1) * 33 + j];         // sender t+1
+#pragma unroll
+          for (int kk = 0; kk < KW; ++kk) {
+            const int t = c.t0 + lane + 32 * kk;
+            // increasing sender order, `<=`: the last minimiser wins
+            float m = __fmaf_rn(fm1, w, cs.hs[t - 1]);
+            int arg = t - 1;
+            const float n0 = __fmaf_rn(f00, w, h[kk]);
+            const float n1 = __fmaf_rn(fp1, w, cs.hs[t + 1]);
+            const bool k0 = n0 <= m;
+            m = k0 ? n0 : m;
+            arg = k0 ? t : arg;
+            const bool k1 = n1 <= m;
+            mw[kk] = k1 ? n1 : m;
+            aw[kk] = k1 ? t + 1 : arg;
+          }
+        } else if (R >= 0) {
+          float fR[5];  // taps of senders t-2 .. t+2
+#pragma unroll
+          for (int q = 0; q < 5; ++q) fR[q] = tile[max(1, min(a.Lv - 1, c0 - (q - 2))) * 33 + j];
 #pragma unroll
           for (int kk = 0; kk < KW; ++kk) {
             const int t = c.t0 + lane + 32 * kk;
             float m = kInf;
             int arg = 0;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+              const int jd = q - 2;
+              const float nm = __fmaf_rn(fR[q], w, cs.hs[t + jd]);
+              const bool take = (jd >= -R) && (jd <= R) && (nm <= m);
+              m = take ? nm : m;
+              arg = take ? t + jd : arg;
+            }
+            mw[kk] = m;
+            aw[kk] = arg;
+          }
+        } else {
+#pragma unroll
+          for (int kk = 0; kk < KW; ++kk) {
+            mw[kk] = kInf;
+            aw[kk] = 0;
+          }
+        }
+#pragma unroll
+        for (int kk = 0; kk < KW; ++kk) {
+          const bool valid = c.t0 + lane + 32 * kk < L;
+          const bool win = valid && mw[kk] <= msg_g;
+          msg[kk] = win ? mw[kk] : msg_g;
+          am[kk] = win ? aw[kk] : argmin_h;
+          own[kk] = win && mw[kk] < msg_g;
+        }
+        if (s1 >= 0) {
+          // a tie with the candidate at a tie-only offset of s1: the last
+          // sender at the candidate value takes the argmin
+          const float hs1 = cs.hs[s1];
+#pragma unroll
+          for (int kk = 0; kk < KW; ++kk) {
+            const int t = c.t0 + lane + 32 * kk;
+            const int jd = s1 - t;
+            const int ajd = jd < 0 ? -jd : jd;
+            const float f = tile[max(1, min(a.Lv - 1, c0 - jd)) * 33 + j];
+            const bool tie = (t < L) && ajd > R && ajd <= delta && __fmaf_rn(f, w, hs1) == msg_g && !(mw[kk] < msg_g);
+            am[kk] = tie ? ((mw[kk] == msg_g) ? max(aw[kk], s1) : s1) : am[kk];
+          }
+        }
+      } else {
+        const bool fast = stereo && delta <= kFastDelta && off == 0.0f;
+        // taps of the zero-offset window: the tap of sender s = t + jd is
+        // clamp(Lv/2 - jd, 1, Lv-1), the same for every label
+        float fj[2 * kFastDelta + 1];
+        if (fast) {
+#pragma unroll
+          for (int q = 0; q <= 2 * kFastDelta; ++q) {
+            const int ti = max(1, min(a.Lv - 1, a.Lv / 2 - (q - kFastDelta)));
+            fj[q] = tile[ti * 33 + j];
+          }
+        }
+#pragma unroll
+        for (int kk = 0; kk < KW; ++kk) {
+          const int t = c.t0 + lane + 32 * kk;
+          const bool valid = t < L;
+          float m = kInf;
+          int arg = 0;
+          if (fast && delta == 3) {
+            // hs holds +inf outside [0, L), which never wins against the
+            // finite global candidate, in place of the clipping
 #pragma unroll
             for (int q = kFastDelta - 3; q <= kFastDelta + 3; ++q) {
               const float nm = __fmaf_rn(fj[q], w, cs.hs[t + q - kFastDelta]);
@@ -549,15 +789,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
               m = take ? nm : m;
               arg = take ? t + q - kFastDelta : arg;
             }
-            wv[kk] = m;
-            wa[kk] = arg;
-          }
-        } else {
-#pragma unroll
-          for (int kk = 0; kk < KW; ++kk) {
-            const int t = c.t0 + lane + 32 * kk;
-            float m = kInf;
-            int arg = 0;
+          } else if (fast) {
 #pragma unroll
             for (int q = 0; q <= 2 * kFastDelta; ++q) {
               const int jd = q - kFastDelta;
@@ -566,17 +798,7 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
               m = take ? nm : m;
               arg = take ? t + jd : arg;
             }
-            wv[kk] = m;
-            wa[kk] = arg;
-          }
-        }
-      } else {
-#pragma unroll
-        for (int kk = 0; kk < KW; ++kk) {
-          const int t = c.t0 + lane + 32 * kk;
-          float m = kInf;
-          int arg = 0;
-          if (t < L) {
+          } else if (valid) {
             int start, stop;
             if (stereo) {
               start = sat_u16(roundf(__fsub_rn(__fadd_rn(static_cast<float>(t - (delta - 1)), off), 1.0f)));
@@ -602,72 +824,101 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
               }
             }
           }
-          wv[kk] = m;
-          wa[kk] = arg;
+          const bool win = valid && m <= msg_g;
+          msg[kk] = win ? m : msg_g;
+          am[kk] = win ? arg : argmin_h;
+          own[kk] = win && m < msg_g;
         }
       }
-      // The global candidate needs only the minimum value of h, which any
-      // reduction order gives exactly; its exp is shared by every label the
-      // window does not win (most of them).
-      float min_h = pm;
-      int argmin_h = plab, tot = pcnt;
-      if (NW > 1) {
-        min_h = cs.red[0];
-#pragma unroll
-        for (int w2 = 1; w2 < NW; ++w2) min_h = fminf(min_h, cs.red[w2]);
-        tot = 0;
-#pragma unroll
-        for (int w2 = 0; w2 < NW; ++w2)
-          if (cs.red[w2] == min_h) {
-            tot += reinterpret_cast<const int*>(cs.red)[4 + w2];
-            argmin_h = reinterpret_cast<const int*>(cs.red)[8 + w2];
-          }
-      }
-      const float msg_g = __fmaf_rn(L2, w, min_h);
+
+      // Exps: the labels below the candidate need their own, every other
+      // label shares the candidate's.  When one slot holds all the own labels
+      // (the usual case) that slot's lanes evaluate them and its other lanes
+      // the candidate, in one lane-parallel pass; otherwise the own values
+      // are packed into the warp's lanes (in label order) with the
+      // candidate after them.
       float e_g;
-      if (!exp_try<kExact>(earg(msg_g), e_g, s_ehi, s_elo)) e_g = static_cast<float>(exp(static_cast<double>(msg_g)));
-      // exact ties of the minimum: the reference tree picks the label
-      if (tot > 1) {
-        float tv[K];
-        int tl[K];
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-          tv[k] = cs.hs[lane + 32 * k];
-          tl[k] = lane + 32 * k;
-        }
-        float mv;
-        tree_argmin<K>(tv, tl, L, lane, mv, argmin_h);
-      }
       bool all_ok = true;
+      unsigned bsel = 0u;
+      int nslot = 0;
+      float xs = msg_g;
 #pragma unroll
       for (int kk = 0; kk < KW; ++kk) {
-        const bool valid = c.t0 + lane + 32 * kk < L;
-        const bool win = valid && wv[kk] <= msg_g;
-        msg[kk] = win ? wv[kk] : msg_g;
-        am[kk] = win ? wa[kk] : argmin_h;
-        e[kk] = valid ? e_g : 0.0f;
-        const bool own = win && wv[kk] != msg_g;
-        if (__any_sync(FULL, own)) {
-          // slot with window winners: their own exp (straight-line code)
-          float ex;
-          const bool okx = exp_try<kExact>(earg(wv[kk]), ex, s_ehi, s_elo);
-          e[kk] = own ? ex : e[kk];
-          all_ok = all_ok && (okx || !own);
-        }
+        const unsigned b = __ballot_sync(FULL, own[kk]);
+        nslot += (b != 0u) ? 1 : 0;
+        bsel = (b != 0u) ? b : bsel;
+        xs = own[kk] ? msg[kk] : xs;
       }
-      if (!__all_sync(FULL, all_ok)) {
-        // rounding undecided in float-float (rare): the reference expression
+      if (nslot <= 1 && bsel != FULL) {
+        float y;
+        const bool okx = exp_try<kExact>(earg(xs), y, s_ehi, s_elo);
+        all_ok = __all_sync(FULL, okx);
+        e_g = __shfl_sync(FULL, y, __ffs(~bsel) - 1);
 #pragma unroll
         for (int kk = 0; kk < KW; ++kk) {
           const bool valid = c.t0 + lane + 32 * kk < L;
-          if (valid && msg[kk] != msg_g) e[kk] = static_cast<float>(exp(static_cast<double>(msg[kk])));
+          e[kk] = own[kk] ? y : (valid ? e_g : 0.0f);
+        }
+      } else {
+        float* eb = cs.erow + c.t0;  // the warp's part of erow (free until the sum)
+        const unsigned lt = (1u << lane) - 1u;
+        int n_own = 0;
+        int pos[KW];
+#pragma unroll
+        for (int kk = 0; kk < KW; ++kk) {
+          const unsigned b = __ballot_sync(FULL, own[kk]);
+          pos[kk] = n_own + __popc(b & lt);
+          if (own[kk] && pos[kk] < 32) eb[pos[kk]] = msg[kk];
+          n_own += __popc(b);
+        }
+        __syncwarp();
+        if (n_own < 32) {
+          const float x = (lane < n_own) ? eb[lane] : msg_g;
+          float y;
+          const bool okx = exp_try<kExact>(earg(x), y, s_ehi, s_elo);
+          all_ok = __all_sync(FULL, lane > n_own || okx);
+          __syncwarp();
+          if (lane < n_own) eb[lane] = y;
+          e_g = __shfl_sync(FULL, y, n_own);
+          __syncwarp();
+#pragma unroll
+          for (int kk = 0; kk < KW; ++kk) {
+            const bool valid = c.t0 + lane + 32 * kk < L;
+            const float eo = eb[own[kk] ? pos[kk] : 0];
+            e[kk] = own[kk] ? eo : (valid ? e_g : 0.0f);
+          }
+        } else {
+          // more than a warp's worth: one pass per slot that has own labels
+          all_ok = exp_try<kExact>(earg(msg_g), e_g, s_ehi, s_elo);
+#pragma unroll
+          for (int kk = 0; kk < KW; ++kk) {
+            const bool valid = c.t0 + lane + 32 * kk < L;
+            e[kk] = valid ? e_g : 0.0f;
+            if (__any_sync(FULL, own[kk])) {
+              float ex;
+              const bool okx = exp_try<kExact>(earg(msg[kk]), ex, s_ehi, s_elo);
+              e[kk] = own[kk] ? ex : e[kk];
+              all_ok = all_ok && (okx || !own[kk]);
+            }
+          }
+          all_ok = __all_sync(FULL, all_ok);
+        }
+        __syncwarp();  // erow is read again only after this step's sum
+      }
+      if (!all_ok) {
+        // rounding undecided in float-float (rare): the reference expression
+        e_g = static_cast<float>(exp(static_cast<double>(msg_g)));
+#pragma unroll
+        for (int kk = 0; kk < KW; ++kk) {
+          const bool valid = c.t0 + lane + 32 * kk < L;
+          e[kk] = own[kk] ? static_cast<float>(exp(static_cast<double>(msg[kk]))) : (valid ? e_g : 0.0f);
         }
       }
     }
 
     if (VARIANT == BPL_LBP_SEM_PIXEL) {
       __syncwarp();
-      if (i + a.ns < nsteps) issue_stage<VARIANT, T>(a, c, sm, lroww, i + a.ns, st, lane);
+      if (st == grp * G + G - 1) issue_group<VARIANT, T>(a, c, sm, lroww, i + 1 - G + a.ns, grp, nsteps, lane);
       if (!a.vec4) cp_async_commit();
     }
 
@@ -700,12 +951,25 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
       const int t = c.t0 + lane + 32 * kk;
       const T o = stf<T>(__fsub_rn(msg[kk], lse));
       chain[kk] = ldf<T>(o);  // the stored value, so the chain matches memory
-      if (t < L) {
-        dstm[t] = o;
-        const int64_t ao = c.out_off + qo + t;
-        if (a.argmin_kind == BPL_ARGMIN_U8) static_cast<uint8_t*>(a.argmin)[ao] = static_cast<uint8_t>(am[kk]);
-        else if (a.argmin_kind == BPL_ARGMIN_F32) static_cast<float*>(a.argmin)[ao] = static_cast<float>(am[kk]);
-        else if (a.argmin_kind == BPL_ARGMIN_U16) static_cast<uint16_t*>(a.argmin)[ao] = static_cast<uint16_t>(am[kk]);
+      if (t < L) dstm[t] = o;
+    }
+    {
+      const int64_t ao = c.out_off + qo;
+      if (a.argmin_kind == BPL_ARGMIN_U8) {
+        uint8_t* d = static_cast<uint8_t*>(a.argmin) + ao;
+#pragma unroll
+        for (int kk = 0; kk < KW; ++kk)
+          if (c.t0 + lane + 32 * kk < L) d[c.t0 + lane + 32 * kk] = static_cast<uint8_t>(am[kk]);
+      } else if (a.argmin_kind == BPL_ARGMIN_U16) {
+        uint16_t* d = static_cast<uint16_t*>(a.argmin) + ao;
+#pragma unroll
+        for (int kk = 0; kk < KW; ++kk)
+          if (c.t0 + lane + 32 * kk < L) d[c.t0 + lane + 32 * kk] = static_cast<uint16_t>(am[kk]);
+      } else if (a.argmin_kind == BPL_ARGMIN_F32) {
+        float* d = static_cast<float*>(a.argmin) + ao;
+#pragma unroll
+        for (int kk = 0; kk < KW; ++kk)
+          if (c.t0 + lane + 32 * kk < L) d[c.t0 + lane + 32 * kk] = static_cast<float>(am[kk]);
       }
     }
     // (float)max((double)sum, 1e-45): the smallest positive float when sum is 0
@@ -720,20 +984,16 @@ __global__ void __launch_bounds__(128) lbp_forward_kernel(FwdArgs a) {
       }
       __syncwarp();
     }
-    if (++st == a.ns) {
-      st = 0;
-      par ^= 1u;
-    }
+    if (kRing && ++st == a.ns) st = 0;
   }
 
-  if (failed && a.vec4 && lane == 0) {
+  if (kRing && failed && a.vec4 && lane == 0) {
     // drain bulk copies still in flight before the warp's shared memory goes
-    // away: every stage issued so far completes one more phase
-    for (int s = 0; s < a.ns; ++s)
-      if (!mbar_try_wait(&sm.bars[s], 0) && !mbar_try_wait(&sm.bars[s], 1))
-        (void)mbar_wait_bounded(&sm.bars[s], 0, 1u << 16);
+    // away: each group's pending phase is the one `par` expects next
+    // (bounded; a group with nothing in flight just runs out the bound)
+    for (int g = 0; g < a.ns / G; ++g) (void)mbar_wait_bounded(&sm.bars[g], (par >> g) & 1u, 1u << 12);
   }
-  if (!a.vec4) cp_async_wait<0>();
+  if (kRing && !a.vec4) cp_async_wait<0>();
 }
 
 // Host-side launch of one phase for one (K, variant, NW) instantiation.
@@ -745,7 +1005,13 @@ int launch_phase(const FwdArgs& a, cudaStream_t stream) {
   // chains per block: up to 4 warps while the block fits in 200 KB
   const int cpb = std::max(1, std::min(4 / NW, static_cast<int>((200 * 1024) / per_chain)));
   const size_t smem = per_chain * cpb;
-  auto kern = lbp_forward_kernel<K, V, NW, T>;
+  // a phase with more scanlines than about 8 warps per SM keeps 4 blocks
+  // resident (registers capped at 128); fewer scanlines run latency-bound
+  // and keep every register they use
+  auto kern = lbp_forward_kernel<K, V, NW, T, 1>;
+  if constexpr (K <= 8) {
+    if (a.nchains > kHiOccChainsPerSm * sm_count()) kern = lbp_forward_kernel<K, V, NW, T, 4>;
+  }
   if (smem > 48 * 1024) {
     if (static_cast<int>(smem) > max_smem_optin())
       return set_error(BPL_ERR_UNSUPPORTED, "lbp_forward: shared memory %zu exceeds device limit", smem);
