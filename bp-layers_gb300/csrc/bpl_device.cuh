@@ -104,8 +104,6 @@ __device__ __forceinline__ float tree_sum(float (&v)[K], int L, int lane) {
   return __shfl_sync(FULL, v0, 0);
 }
 
-// Plain warp sum (any order) for the adjoint kernels, which have no bitwise
-// parity target (the reference uses float atomics).
 // Order-preserving map of floats onto unsigned integers (-0 below +0, NaN
 // above +inf), so that a warp minimum is one redux.sync instruction.
 __device__ __forceinline__ unsigned f2ord(float f) {
@@ -117,6 +115,34 @@ __device__ __forceinline__ float ord2f(unsigned u) {
 }
 __device__ __forceinline__ float warp_min_redux(float v) { return ord2f(__reduce_min_sync(0xffffffffu, f2ord(v))); }
 
+// Reduce-scatter of 8 per-lane values over the warp in 9 shuffles (instead
+// of 8 full warp sums): returns in every lane the warp total of value
+// (lane >> 2) & 7, i.e. lanes 4b..4b+3 hold the total of value b.  Any
+// summation order (for the adjoint kernels, which have no bitwise target).
+__device__ __forceinline__ float warp_reduce_scatter8(const float (&v)[8], int lane) {
+  const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4;
+  float w4[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float keep = h16 ? v[i + 4] : v[i];
+    const float send = h16 ? v[i] : v[i + 4];
+    w4[i] = keep + __shfl_xor_sync(FULL, send, 16);
+  }
+  float w2[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const float keep = h8 ? w4[i + 2] : w4[i];
+    const float send = h8 ? w4[i] : w4[i + 2];
+    w2[i] = keep + __shfl_xor_sync(FULL, send, 8);
+  }
+  float w1 = (h4 ? w2[1] : w2[0]) + __shfl_xor_sync(FULL, h4 ? w2[0] : w2[1], 4);
+  w1 += __shfl_xor_sync(FULL, w1, 2);
+  w1 += __shfl_xor_sync(FULL, w1, 1);
+  return w1;
+}
+
+// Plain warp sum (any order) for the adjoint kernels, which have no bitwise
+// parity target (the reference uses float atomics).
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);

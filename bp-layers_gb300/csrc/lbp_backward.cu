@@ -77,7 +77,7 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
     a.vec4 = 1;
   }
   a.am_bulk = (a.vec4 && (Ls * am_size) % 16 == 0) ? 1 : 0;
-  a.ns = kBwdRingCpAsync;
+  a.ns = 0;  // rows are prefetched into registers: no shared-memory ring
   if (storage == 1)
     return (variant == BPL_LBP_STEREO) ? lbp_backward_stereo_f16(a, s) : lbp_backward_sem_pixel_f16(a, s);
   switch (variant) {

@@ -115,8 +115,15 @@ __device__ __forceinline__ float bldf<float>(float v) { return v; }
 template <>
 __device__ __forceinline__ float bldf<__half>(__half v) { return __half2float(v); }
 
+// The vertical phase (one scanline per column) runs 2-warp blocks, 9 of
+// them resident per SM, so that a full-width image's columns fit one wave;
+// the horizontal phase is latency-bound and keeps its registers.
+template <bool CROSS, int K>
+constexpr int bwd_warps_per_block() { return (CROSS || K > 8) ? 4 : 2; }
+
 template <int K, int VARIANT, int LV, bool CROSS, typename T>
-__global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
+__global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS || K > 8) ? 1 : 9)
+    lbp_backward_kernel(BwdArgs a) {
   using namespace bwd;
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
@@ -186,72 +193,73 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   if (VARIANT == BPL_LBP_SEM_GLOBAL)
     for (int t = lane; t < L * L; t += 32) sm.jacc[t] = 0.0f;
 
-  // stage rows: messages (T), in_grad (T), saved UP, saved DOWN (float), argmin
-  const int lr = a.lrow;
-  const int tfl = lr * static_cast<int>(sizeof(T)) / 4;  // floats per T row
-  auto issue = [&](int k, int st) {
-    float* dst = sm.ring + st * stage_floats(lr, sizeof(T));
+  // The next step's rows (messages and in_grad as T, the argmin, the saved
+  // vertical gradients) are prefetched into registers one step ahead:
+  // coalesced loads of data no sweep of this phase writes.  They stay raw
+  // until used, so the loads do not stall the step that issues them.
+  T pm_[K], pg_[K];
+  uint32_t pa_[K];
+  float pu_[K], pd_[K];
+  auto prefetch = [&](int k) {
     const int64_t qo = static_cast<int64_t>(pin0 + k * dpin + dq) * Ls;
-    if (a.vec4) {
-      if (lane == 0) {
-        const uint32_t rt = static_cast<uint32_t>(Ls) * static_cast<uint32_t>(sizeof(T));
-        const uint32_t rf = static_cast<uint32_t>(Ls) * 4u;
-        const uint32_t ab = a.am_bulk ? static_cast<uint32_t>(Ls) * am_size : 0u;
-        fence_proxy_async();
-        mbar_arrive_expect_tx(&sm.bars[st], 2u * rt + (CROSS ? 2u * rf : 0u) + ab);
-        bulk_g2s(dst, msgs_db + qo, rt, &sm.bars[st]);
-        bulk_g2s(dst + tfl, grad_db + qo, rt, &sm.bars[st]);
-        if (CROSS) {
-          bulk_g2s(dst + 2 * tfl, saved_up + qo, rf, &sm.bars[st]);
-          bulk_g2s(dst + 2 * tfl + lr, saved_dn + qo, rf, &sm.bars[st]);
-        }
-        if (a.am_bulk) bulk_g2s(dst + 2 * tfl + 2 * lr, am_db + qo * am_size, ab, &sm.bars[st]);
-      }
-    } else if constexpr (sizeof(T) == 4) {
-      // rows not 16-byte sized (float storage only; half rows are padded)
-      for (int t = lane; t < L; t += 32) {
-        cp_async4(dst + t, msgs_db + qo + t);
-        cp_async4(dst + tfl + t, grad_db + qo + t);
-        if (CROSS) {
-          cp_async4(dst + 2 * tfl + t, saved_up + qo + t);
-          cp_async4(dst + 2 * tfl + lr + t, saved_dn + qo + t);
-        }
+    if (a.argmin_kind == BPL_ARGMIN_U8) {
+      const uint8_t* ab = am_db + qo;
+#pragma unroll
+      for (int kk = 0; kk < K; ++kk) pa_[kk] = __ldg(ab + ((lane + 32 * kk < L) ? lane + 32 * kk : 0));
+    } else if (a.argmin_kind == BPL_ARGMIN_U16) {
+      const uint16_t* ab = reinterpret_cast<const uint16_t*>(am_db) + qo;
+#pragma unroll
+      for (int kk = 0; kk < K; ++kk) pa_[kk] = __ldg(ab + ((lane + 32 * kk < L) ? lane + 32 * kk : 0));
+    } else {
+      const float* ab = reinterpret_cast<const float*>(am_db) + qo;
+#pragma unroll
+      for (int kk = 0; kk < K; ++kk)
+        pa_[kk] = __float_as_uint(__ldg(ab + ((lane + 32 * kk < L) ? lane + 32 * kk : 0)));
+    }
+#pragma unroll
+    for (int kk = 0; kk < K; ++kk) {
+      const int t = lane + 32 * kk;
+      const int64_t o = qo + ((t < L) ? t : 0);  // labels >= L read label 0 (ignored)
+      pm_[kk] = __ldg(msgs_db + o);
+      pg_[kk] = __ldg(grad_db + o);
+      if (CROSS) {
+        pu_[kk] = __ldg(saved_up + o);
+        pd_[kk] = __ldg(saved_dn + o);
       }
     }
   };
 
   // per-step tile: stereo taps (Lv rows), edge weight (row Lv), scale (row Lv+1)
   const int trow = a.Lv + 2;
-  auto load_tile_regs = [&](int b, float (&rg)[18]) {
-    const int k = 32 * b + lane;
-    if (k >= nsteps) return;
+  // Loaded 32 steps ahead and written to the tile when its block starts; the
+  // registers are not read before then, so the loads never stall a step.
+  // Constant register indices (a run-time index would put rg on the stack).
+  float ev = 0.0f, sv = 0.0f;
+  auto load_tile_regs = [&](int b, float (&rg)[16]) {
+    const int k = min(32 * b + lane, nsteps - 1);  // lanes past the end reload the last step
     const int p = pin0 + k * dpin;
-    rg[a.Lv] = __ldg(edge_fd + p);
-    rg[a.Lv + 1] = __ldg(scale_db + p + dq);
+    ev = __ldg(edge_fd + p);
+    sv = __ldg(scale_db + p + dq);
     if (stereo) {
 #pragma unroll
       for (int j = 0; j < 16; ++j)
         if (j < a.Lv) rg[j] = __ldg(jump_fd + static_cast<int64_t>(j) * HW + p);
     }
   };
-  auto store_tile = [&](float* tile, const float (&rg)[18]) {
+  auto store_tile = [&](float* tile, const float (&rg)[16]) {
+    if (stereo) {
 #pragma unroll
-    for (int j = 0; j < 18; ++j)
-      if (j < trow) tile[j * 33 + lane] = rg[j];
+      for (int j = 0; j < 16; ++j)
+        if (j < a.Lv) tile[j * 33 + lane] = rg[j];
+    }
+    tile[a.Lv * 33 + lane] = ev;
+    tile[(a.Lv + 1) * 33 + lane] = sv;
   };
 
-  if (a.vec4 && lane == 0) {
-    for (int s = 0; s < a.ns; ++s) mbar_init(&sm.bars[s], 1);
-    fence_mbar_init();
-  }
-  __syncwarp();
-  for (int k = 0; k < a.ns; ++k) {
-    if (k < nsteps) issue(k, k);
-    if (!a.vec4) cp_async_commit();
-  }
-  float rg[18];
+  prefetch(0);
+  float rg[16];
 #pragma unroll
-  for (int j = 0; j < 18; ++j) rg[j] = 0.0f;
+  for (int j = 0; j < 16; ++j) rg[j] = 0.0f;
   load_tile_regs(0, rg);
   store_tile(sm.tile, rg);
   if (nsteps > 32) load_tile_regs(1, rg);
@@ -263,67 +271,46 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
   float* rowH = sm.rows;
   float* rowU = sm.rows + 32 * K;
   float* rowD = sm.rows + 64 * K;
-  const int sf = stage_floats(lr, sizeof(T));
+  const bool am_f32 = a.argmin_kind == BPL_ARGMIN_F32;
 
-  bool failed = false;
-  int st = 0;
-  uint32_t par = 0;
   int p = pin0;
   for (int k = 0; k < nsteps; ++k, p += dpin) {
     const int j = k & 31;
     const int b = k >> 5;
     const float* tile = sm.tile + (b & 1) * (trow * 33);
-    const float* stg = sm.ring + st * sf;
-    const int64_t qo = static_cast<int64_t>(p + dq) * Ls;
-
-    if (a.vec4) {
-      const bool ok = mbar_wait_bounded(&sm.bars[st], par);
-      if (!__all_sync(FULL, ok)) { failed = true; break; }
-    } else {
-      cp_async_wait<kBwdRingCpAsync - 1>();
-      __syncwarp();
-    }
 
     const float w = tile[a.Lv * 33 + j];
     const float inv_s = (sizeof(T) == 4) ? 1.0f : __frcp_rn(tile[(a.Lv + 1) * 33 + j]);
     float g[K], pr[K], sU[K], sD[K];
     int am[K];
     float sg = 0.0f, sa = 0.0f;
-    const T* m_row = reinterpret_cast<const T*>(stg);
-    const T* g_row = reinterpret_cast<const T*>(stg + tfl);
-    const float* su_row = stg + 2 * tfl;
-    const float* sd_row = su_row + lr;
-    const void* amrow = a.am_bulk ? static_cast<const void*>(sd_row + lr)
-                                  : static_cast<const void*>(am_db + qo * am_size);
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
-      const int t = lane + 32 * kk;
-      const bool valid = t < L;
-      int s = 0;
-      if (valid) {
-        if (a.argmin_kind == BPL_ARGMIN_U8) s = static_cast<const uint8_t*>(amrow)[t];
-        else if (a.argmin_kind == BPL_ARGMIN_U16) s = static_cast<const uint16_t*>(amrow)[t];
-        else s = static_cast<int>(static_cast<const float*>(amrow)[t]);
-      }
-      am[kk] = s;
-      g[kk] = valid ? bldf<T>(g_row[t]) : 0.0f;
+      const bool valid = lane + 32 * kk < L;
+      am[kk] = valid ? (am_f32 ? static_cast<int>(__uint_as_float(pa_[kk])) : static_cast<int>(pa_[kk])) : 0;
+      g[kk] = valid ? bldf<T>(pg_[kk]) : 0.0f;
       // exp(m + log S) / S of the reference (:328-341) is exp(m) for a
-      // normalised message m = m_raw - log S
       // normalised message m = m_raw - log S; half rows hold m_raw - min h
       // with their scale the sum of exp of the row, so exp(m) = exp(row) / scale
-      pr[kk] = valid ? (sizeof(T) == 4 ? expf(bldf<T>(m_row[t])) : __expf(bldf<T>(m_row[t])) * inv_s) : 0.0f;
-      sU[kk] = (CROSS && valid) ? su_row[t] : 0.0f;
-      sD[kk] = (CROSS && valid) ? sd_row[t] : 0.0f;
+      pr[kk] = valid ? __expf(bldf<T>(pm_[kk])) * inv_s : 0.0f;
+      sU[kk] = (CROSS && valid) ? pu_[kk] : 0.0f;
+      sD[kk] = (CROSS && valid) ? pd_[kk] : 0.0f;
       sg += g[kk];
       sa += accH[kk];
     }
-    // stage consumed: refill with step k + ns
-    __syncwarp();
-    if (k + a.ns < nsteps) issue(k + a.ns, st);
-    if (!a.vec4) cp_async_commit();
+    if (k + 1 < nsteps) prefetch(k + 1);
 
-    sg = warp_sum(sg);
-    sa = warp_sum(sa);
+    // both sums in one reduce-scatter: lanes < 16 end with sum(g), the
+    // others with sum(accH)
+    {
+      float v = (lane & 16) ? sa : sg;
+      const float o = __shfl_xor_sync(FULL, (lane & 16) ? sg : sa, 16);
+      v += o;
+#pragma unroll
+      for (int o2 = 8; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(FULL, v, o2);
+      sg = __shfl_sync(FULL, v, 0);
+      sa = __shfl_sync(FULL, v, 16);
+    }
     float addH[K], addU[K], addD[K];
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
@@ -346,44 +333,41 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const bool v = lane + 32 * kk < L;
-      c0 += __popc(__ballot_sync(FULL, v && am[kk] == g0));
-      cL += __popc(__ballot_sync(FULL, v && am[kk] == gL));
+      c0 += (v && am[kk] == g0) ? 1 : 0;
+      cL += (v && am[kk] == gL) ? 1 : 0;
     }
+    c0 = __reduce_add_sync(FULL, c0);
+    cL = __reduce_add_sync(FULL, cL);
     const int gd = (c0 >= cL) ? g0 : gL;
-    float dh = 0.0f, du = 0.0f, dd = 0.0f;
+    float dsum[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) dsum[q] = 0.0f;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const bool v = lane + 32 * kk < L;
       const bool dom = v && am[kk] == gd;
-      dh += dom ? addH[kk] : 0.0f;
+      dsum[0] += dom ? addH[kk] : 0.0f;
       if (CROSS) {
-        du += dom ? addU[kk] : 0.0f;
-        dd += dom ? addD[kk] : 0.0f;
+        dsum[1] += dom ? addU[kk] : 0.0f;
+        dsum[2] += dom ? addD[kk] : 0.0f;
       }
-      if (v && !dom) {
-        atomicAdd(&rowH[am[kk]], addH[kk]);
-        if (CROSS) {
-          atomicAdd(&rowU[am[kk]], addU[kk]);
-          atomicAdd(&rowD[am[kk]], addD[kk]);
+      const bool nd = v && !dom;
+      if (__any_sync(FULL, nd)) {
+        if (nd) {
+          atomicAdd(&rowH[am[kk]], addH[kk]);
+          if (CROSS) {
+            atomicAdd(&rowU[am[kk]], addU[kk]);
+            atomicAdd(&rowD[am[kk]], addD[kk]);
+          }
         }
       }
     }
-    dh = warp_sum(dh);
-    if (CROSS) {
-      du = warp_sum(du);
-      dd = warp_sum(dd);
-    }
-    if (lane == 0) {
-      rowH[gd] += dh;  // no other lane touches label gd
-      if (CROSS) {
-        rowU[gd] += du;
-        rowD[gd] += dd;
-      }
-    }
 
-    // pairwise and edge gradients
+    // pairwise and edge gradients: per-tap sums of the total contribution,
+    // tap index clamp(Lv/2 + t - s*), reduced together with the dominant
+    // group's sums (tap bins in values 3..7 for Lv <= 6, else a second pass)
+    float ge = 0.0f;
     if (stereo) {
-      // per-tap sums of the total contribution; tap index clamp(Lv/2 + t - s*)
       constexpr int NB = (LV > 0) ? LV : 16;
       const int lv = (LV == 6 || LV == 8) ? LV : a.Lv;
       float bins[NB];
@@ -398,18 +382,46 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
         for (int bb = 1; bb < NB; ++bb)
           if (LV == 6 || LV == 8 || bb < lv) bins[bb] += (ti == bb) ? tot : 0.0f;
       }
-      float ge = 0.0f;
+      if (LV == 6) {
+        // values 0..2: dominant sums, 3..7: taps 1..5
 #pragma unroll
-      for (int bb = 1; bb < NB; ++bb) {
-        if (LV == 6 || LV == 8 || bb < lv) {
-          const float v = warp_sum(bins[bb]);
-          ge += tile[bb * 33 + j] * v;
-          if (lane == bb && v != 0.0f) atomicAdd(gjump_fd + static_cast<int64_t>(bb) * HW + p, w * v);
+        for (int bb = 1; bb < 6; ++bb) dsum[2 + bb] = bins[bb];
+        const float r = warp_reduce_scatter8(dsum, lane);
+        const int q = (lane >> 2) & 7;
+        if ((lane & 3) == 0 && q >= 3) {
+          const int bb = q - 2;
+          ge = tile[bb * 33 + j] * r;
+          if (r != 0.0f) atomicAdd(gjump_fd + static_cast<int64_t>(bb) * HW + p, w * r);
+        }
+        if (lane == 0) rowH[gd] += r;  // no other lane touches label gd
+        if (CROSS && lane == 4) rowU[gd] += r;
+        if (CROSS && lane == 8) rowD[gd] += r;
+      } else {
+        const float r = warp_reduce_scatter8(dsum, lane);
+        if (lane == 0) rowH[gd] += r;
+        if (CROSS && lane == 4) rowU[gd] += r;
+        if (CROSS && lane == 8) rowD[gd] += r;
+        // taps 1..NB-1 in passes of 8
+#pragma unroll
+        for (int b0 = 0; b0 < NB; b0 += 8) {
+          float tv[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) tv[q] = (b0 + q >= 1 && b0 + q < NB) ? bins[(b0 + q < NB) ? b0 + q : 0] : 0.0f;
+          const float rb = warp_reduce_scatter8(tv, lane);
+          const int bb = b0 + ((lane >> 2) & 7);
+          if ((lane & 3) == 0 && bb >= 1 && bb < lv) {
+            ge += tile[bb * 33 + j] * rb;
+            if (rb != 0.0f) atomicAdd(gjump_fd + static_cast<int64_t>(bb) * HW + p, w * rb);
+          }
         }
       }
+      ge = warp_sum(ge);
       if (lane == 0 && ge != 0.0f) atomicAdd(gedge_fd + p, ge);
     } else {
-      float ge = 0.0f;
+      const float r = warp_reduce_scatter8(dsum, lane);
+      if (lane == 0) rowH[gd] += r;
+      if (CROSS && lane == 4) rowU[gd] += r;
+      if (CROSS && lane == 8) rowD[gd] += r;
 #pragma unroll
       for (int kk = 0; kk < K; ++kk) {
         const int t = lane + 32 * kk;
@@ -433,25 +445,24 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
     __syncwarp();
 
     // read back the chain accumulators (and clear the rows for the next
-    // step); grad_cost[p][s] receives rowH + rowU + rowD
+    // step); grad_cost[p][s] receives rowH + rowU + rowD.  The rows are 32K
+    // long, so labels >= L read zeros.
     float* gc = gcost_n + static_cast<int64_t>(p) * Ls;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const int t = lane + 32 * kk;
-      if (t < L) {
-        accH[kk] = rowH[t];
-        rowH[t] = 0.0f;
-        float v = accH[kk];
-        if (CROSS) {
-          accU[kk] = rowU[t];
-          accD[kk] = rowD[t];
-          rowU[t] = 0.0f;
-          rowD[t] = 0.0f;
-          v = (v + accU[kk]) + accD[kk];
-        }
-        if (v != 0.0f) atomicAdd(gc + t, v);
-        if (!CROSS) saved_out[static_cast<int64_t>(p) * Ls + t] = accH[kk];
+      accH[kk] = rowH[t];
+      rowH[t] = 0.0f;
+      float v = accH[kk];
+      if (CROSS) {
+        accU[kk] = rowU[t];
+        accD[kk] = rowD[t];
+        rowU[t] = 0.0f;
+        rowD[t] = 0.0f;
+        v = (v + accU[kk]) + accD[kk];
       }
+      if (t < L && v != 0.0f) atomicAdd(gc + t, v);
+      if (!CROSS && t < L) saved_out[static_cast<int64_t>(p) * Ls + t] = accH[kk];
     }
 
     if (j == 31 || k == nsteps - 1) {
@@ -462,10 +473,6 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
       }
     }
     __syncwarp();
-    if (++st == a.ns) {
-      st = 0;
-      par ^= 1u;
-    }
   }
 
   if (VARIANT == BPL_LBP_SEM_GLOBAL) {
@@ -477,22 +484,17 @@ __global__ void __launch_bounds__(128) lbp_backward_kernel(BwdArgs a) {
       if (v != 0.0f) atomicAdd(a.grad_jump + static_cast<int64_t>(fd) * L * L + t, v);
     }
   }
-  if (failed && a.vec4 && lane == 0) {
-    for (int s = 0; s < a.ns; ++s)
-      if (!mbar_try_wait(&sm.bars[s], 0) && !mbar_try_wait(&sm.bars[s], 1))
-        (void)mbar_wait_bounded(&sm.bars[s], 0, 1u << 16);
-  }
-  if (!a.vec4) cp_async_wait<0>();
 }
 
 template <int K, int V, int LV, typename T>
 int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
   BwdArgs a = a0;
   const int per_warp = bwd::warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, V, sizeof(T)) * 4;
-  const int wpb = std::max(1, std::min(4, (200 * 1024) / per_warp));
-  const size_t smem = static_cast<size_t>(per_warp) * wpb;
   for (int phase = 0; phase < 2; ++phase) {
     auto kern = (phase == 0) ? lbp_backward_kernel<K, V, LV, false, T> : lbp_backward_kernel<K, V, LV, true, T>;
+    const int wmax = (phase == 0) ? bwd_warps_per_block<false, K>() : bwd_warps_per_block<true, K>();
+    const int wpb = std::max(1, std::min(wmax, (200 * 1024) / per_warp));
+    const size_t smem = static_cast<size_t>(per_warp) * wpb;
     if (smem > 48 * 1024) {
       if (static_cast<int>(smem) > max_smem_optin())
         return set_error(BPL_ERR_UNSUPPORTED, "lbp_backward: shared memory %zu exceeds device limit", smem);
