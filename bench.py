@@ -294,6 +294,8 @@ def run_ours(args):
         "fp16": fp16,
         "clocks": clk.summary(),
     }
+    if world == 1 and not args.no_serving:
+        result["serving"] = run_serving(args)
     traffic = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic):
         with open(traffic) as fh:
@@ -307,6 +309,67 @@ def run_ours(args):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(result))
+
+
+SERVE_MIX = [((376, 1240, 128), 0.5), ((540, 960, 192), 0.3), ((720, 1280, 256), 0.2)]
+SERVE_C = 64
+
+
+def run_serving(args):
+    """Served mixed stream of stereo requests (SAD + 3-iteration FP16-storage
+    BP forward + disparity): Poisson arrivals (seed 1) over the shape mix,
+    served by the continuous-batching engine (free-HBM admission, resident
+    volumes, captured graphs), against plain per-request launches of the
+    same requests.  Plain capacity is measured first (requests back to
+    back); the stream is then offered at `serve_load` times that capacity
+    to both, in real time."""
+    import numpy as np
+    import torch
+    from bpl_gb300 import serving
+    dev = torch.device("cuda", 0)
+    n = args.serve_requests
+    g = np.random.default_rng(1)
+    shapes = [s for s, _ in SERVE_MIX]
+    probs = np.array([w for _, w in SERVE_MIX])
+    kinds = g.choice(len(shapes), size=n, p=probs / probs.sum())
+    feats = {}
+    for k in range(len(shapes)):  # two distinct scenes per shape, reused
+        H_, W_, D_ = shapes[k]
+        feats[k] = [serving.synth_request_features(H_, W_, D_, SERVE_C, seed=10 * k + j, device=dev) for j in range(2)]
+
+    def make(arrivals):
+        return [serving.StereoRequest(i, *feats[int(kinds[i])][i % 2], shapes[int(kinds[i])][2], arrival=float(a))
+                for i, a in enumerate(arrivals)]
+
+    # plain capacity: back to back (after one warm-up request per shape)
+    serving.run_plain([serving.StereoRequest(-1 - k, *feats[k][0], shapes[k][2]) for k in range(len(shapes))],
+                      realtime=False)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    serving.run_plain(make(np.zeros(n)), realtime=False)
+    plain_rps = n / (time.perf_counter() - t)
+    rate = args.serve_load * plain_rps
+    arrivals = np.cumsum(g.exponential(1.0 / rate, size=n))
+    plain = serving.latency_stats(serving.run_plain(make(arrivals)))
+    eng = serving.ServingEngine(shapes, C=SERVE_C, max_batch=4, hbm_fraction=0.5, weights=probs, device=dev)
+    eng.warm_up()
+    served_reqs = eng.serve(make(arrivals))
+    served = serving.latency_stats(served_reqs)
+    torch.cuda.synchronize()
+    plan = eng.plan
+    eng = None
+    torch.cuda.empty_cache()
+    return {
+        "requests": n, "mix": [{"H": s[0], "W": s[1], "D": s[2], "p": w} for s, w in SERVE_MIX],
+        "pipeline": "SAD (C=64) + softmax + 3-iteration FP16-storage BP forward + disparity argmin",
+        "offered_rate_rps": rate, "offered_load_vs_plain_capacity": args.serve_load,
+        "plain_capacity_rps": plain_rps,
+        "served": {"requests_per_s": served["requests_per_s"], "p50_ms": served["p50_ms"], "p99_ms": served["p99_ms"]},
+        "plain": {"requests_per_s": plain["requests_per_s"], "p50_ms": plain["p50_ms"], "p99_ms": plain["p99_ms"]},
+        "throughput_vs_plain": (served["requests_per_s"] / plain["requests_per_s"]
+                                if served["requests_per_s"] and plain["requests_per_s"] else None),
+        "slot_plan": {f"{s[0]}x{s[1]}x{s[2]}": {"sets": v[0], "batch": v[1]} for s, v in plan.items()},
+    }
 
 
 def cpu_sample_inputs(wc=CPU_CROP_W):
@@ -410,9 +473,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp16", action="store_true", help="skip the FP16-storage leg")
     ap.add_argument("--ncu-case", action="store_true", help="small case for ncu captures")
+    ap.add_argument("--no-serving", action="store_true", help="skip the served-stream leg")
+    ap.add_argument("--serving-only", action="store_true", help="run only the served-stream leg")
+    ap.add_argument("--serve-requests", type=int, default=40)
+    ap.add_argument("--serve-load", type=float, default=4.0,
+                    help="offered arrival rate as a multiple of the plain per-request capacity")
     args = ap.parse_args()
     if args.ncu_case:
         run_ncu_case(args)
+    elif args.serving_only:
+        print(json.dumps(run_serving(args)))
     elif args.impl == "reference":
         run_reference(args)
     else:

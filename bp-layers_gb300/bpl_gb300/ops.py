@@ -300,8 +300,9 @@ def lbp_forward_f16(variant: int, cost_h: torch.Tensor, jump: torch.Tensor, edge
             raise BplError(f"pixel jump must be (4,H,W,L,Lp) half, got {tuple(jump.shape)}")
     else:
         raise BplError("FP16 storage serves the stereo and pixel variants")
-    kind = _ARGMIN_KIND[argmin_dtype]
-    if argmin is None:
+    # argmin_dtype=None: no argmin is written (inference)
+    kind = ARGMIN_NONE if argmin_dtype is None else _ARGMIN_KIND[argmin_dtype]
+    if argmin is None and kind != ARGMIN_NONE:
         argmin = torch.zeros((B, 4, H, W, Lp), dtype=argmin_dtype, device=cost_h.device)
     if scale is None:
         scale = torch.zeros((B, 4, H, W), dtype=torch.float32, device=cost_h.device)
