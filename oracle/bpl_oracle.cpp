@@ -31,6 +31,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -265,14 +266,34 @@ void lbp_forward(int variant, const T* cost, const T* jump, const T* edge, T* ms
 //   global  (B,4,L,L)      [reference writes batch 0 only, :395-397]
 //   pixel   (4,H,W,L,L)
 // Edge gradient: (B,4,H,W) per batch item; pixel has none.
-void lbp_backward_ref(int variant, const float* jump, const float* edge, const float* in_grad,
-                      const float* msgs, const float* argmin, const float* scale, double* g_cost,
-                      double* g_jump, double* g_edge, double* g_msgs, int B, int H, int W, int L,
-                      int Lv, int jb, int eb, int threads) {
+// Reference adjoint (exact = false) and exact adjoint (exact = true) of one
+// pass.  The exact adjoint is the reverse-mode derivative of the forward
+// pass as written: sweeps undone in reverse order (UP, DOWN, then LEFT,
+// RIGHT; each orientation's two sweeps are independent), every step taking
+// a = (upstream gradient of the message) + (gradients of its later readers)
+// through J^T = I - p 1^T of the log normalisation and scattering it to h of
+// the sender by argmin.  A horizontal message's later readers are the next
+// step of its sweep (acc) and the two vertical sweeps at the receiver (the
+// saved vertical accumulators); the reference instead carries the vertical
+// parts as separate accumulators without J^T and returns in_grad as the
+// message gradient (lbp_min_sum_kernel.cu:380-386, :534-536).  The exact
+// message gradient is with respect to the pass's input messages: the old
+// vertical messages read by the horizontal sweeps, the chain inputs at each
+// sweep's first sender, and the upstream gradient of slots the pass never
+// writes (those values pass through).
+template <typename T>
+void lbp_backward_t(int variant, bool exact, const T* jump, const T* edge, const T* in_grad,
+                    const T* msgs, const float* argmin, const T* scale, double* g_cost,
+                    double* g_jump, double* g_edge, double* g_msgs, int B, int H, int W, int L,
+                    int Lv, int jb, int eb, int threads) {
   Shape S{B, H, W, L};
-  PairwiseT<float> P{variant, Lv, jb, H, W, L, jump};
+  PairwiseT<T> P{variant, Lv, jb, H, W, L, jump};
   const int64_t nmsg = static_cast<int64_t>(B) * 4 * H * W * L;
-  for (int64_t i = 0; i < nmsg; ++i) g_msgs[i] = in_grad[i];
+  if (!exact) {
+    for (int64_t i = 0; i < nmsg; ++i) g_msgs[i] = in_grad[i];
+  } else {
+    for (int64_t i = 0; i < nmsg; ++i) g_msgs[i] = 0.0;
+  }
   std::vector<double> saved(nmsg, 0.0);
 #ifdef _OPENMP
   if (threads > 0) omp_set_num_threads(threads);
@@ -288,37 +309,45 @@ void lbp_backward_ref(int variant, const float* jump, const float* edge, const f
       const int len = horiz ? W : H;
 #pragma omp parallel
       {
-        std::vector<double> acc(3 * L), nacc(3 * L), p(L);
+        std::vector<double> acc(3 * L), nacc(3 * L), p(L), a(L);
         // the global-pairwise gradient is shared by every chain: accumulate
         // per thread, then reduce
         std::vector<double> gj_local(variant == VAR_SEM_GLOBAL ? static_cast<size_t>(L) * L : 0, 0.0);
 #pragma omp for schedule(dynamic, 1)
         for (int ch = 0; ch < nchains; ++ch) {
           std::fill(acc.begin(), acc.end(), 0.0);
+          int ly = 0, lx = 0;
           for (int k = 0; k < len - 1; ++k) {
             int y, x, qy, qx;
             if (db == DOWN) { x = ch; y = 1 + k; qy = y - 1; qx = x; }
             else if (db == UP) { x = ch; y = H - 2 - k; qy = y + 1; qx = x; }
             else if (db == LEFT) { y = ch; x = W - 2 - k; qy = y; qx = x + 1; }
             else { y = ch; x = 1 + k; qy = y; qx = x - 1; }
-            const float* m = msgs + S.msg(n, db, qy, qx);
-            const float* g = in_grad + S.msg(n, db, qy, qx);
+            ly = y;
+            lx = x;
+            const T* m = msgs + S.msg(n, db, qy, qx);
+            const T* g = in_grad + S.msg(n, db, qy, qx);
             const float* am = argmin + S.msg(n, db, qy, qx);
             const double sc = scale[S.dir(n, db, qy, qx)];
-            const float lsc = std::log(static_cast<float>(sc));
+            const double lsc = std::is_same<T, float>::value
+                                   ? static_cast<double>(std::log(static_cast<float>(sc)))
+                                   : std::log(sc);
             double sg = 0.0, sa = 0.0;
             for (int c = 0; c < L; ++c) {
-              p[c] = std::exp(static_cast<double>(m[c] + lsc)) / sc;
-              sg += g[c];
+              p[c] = std::exp(static_cast<double>(m[c]) + lsc) / sc;
+              a[c] = g[c];
+              if (exact && cross)
+                a[c] += saved[S.msg(n, UP, qy, qx) + c] + saved[S.msg(n, DOWN, qy, qx) + c];
+              sg += a[c];
               sa += acc[c];
             }
             const double w = edge[S.dir(eb == 1 ? 0 : n, fd, y, x)];
             std::fill(nacc.begin(), nacc.end(), 0.0);
             double ge = 0.0;
             for (int c = 0; c < L; ++c) {
-              const double add_h = (g[c] - p[c] * sg) + (acc[c] - p[c] * sa);
+              const double add_h = (a[c] - p[c] * sg) + (acc[c] - p[c] * sa);
               double add_u = 0.0, add_d = 0.0;
-              if (cross) {
+              if (cross && !exact) {
                 add_u = saved[S.msg(n, UP, qy, qx) + c] + acc[L + c];
                 add_d = saved[S.msg(n, DOWN, qy, qx) + c] + acc[2 * L + c];
               }
@@ -327,7 +356,7 @@ void lbp_backward_ref(int variant, const float* jump, const float* edge, const f
               g_cost[S.pix(n, y, x) * L + s] += tot;
               const double fv = P.f(n, fd, y, x, c, s);
               if (variant == VAR_STEREO) {
-                const int k2 = PairwiseT<float>::tap_index(c, s, Lv);
+                const int k2 = PairwiseT<T>::tap_index(c, s, Lv);
                 g_jump[((((static_cast<int64_t>(n) * 4 + fd) * Lv + k2) * H + y) * W + x)] += w * tot;
                 ge += fv * tot;
               } else if (variant == VAR_SEM_GLOBAL) {
@@ -347,6 +376,23 @@ void lbp_backward_ref(int variant, const float* jump, const float* edge, const f
             acc.swap(nacc);
             double* sv = saved.data() + S.msg(n, db, y, x);
             for (int c = 0; c < L; ++c) sv[c] = acc[c];
+            if (exact && cross) {
+              // h of a horizontal sweep reads the pass's input vertical messages
+              for (int c = 0; c < L; ++c) {
+#pragma omp atomic
+                g_msgs[S.msg(n, UP, y, x) + c] += acc[c];
+#pragma omp atomic
+                g_msgs[S.msg(n, DOWN, y, x) + c] += acc[c];
+              }
+            }
+          }
+          if (exact && len > 1) {
+            // the chain input at the sweep's first sender (the last step here)
+            double* gi = g_msgs + S.msg(n, db, ly, lx);
+            for (int c = 0; c < L; ++c) {
+#pragma omp atomic
+              gi[c] += acc[c];
+            }
           }
         }
         if (variant == VAR_SEM_GLOBAL) {
@@ -356,7 +402,33 @@ void lbp_backward_ref(int variant, const float* jump, const float* edge, const f
         }
       }
     }
+    if (exact) {
+      // slots the pass never writes pass their input through: LEFT at x=0,
+      // RIGHT at x=W-1, UP at y=0, DOWN at y=H-1; the vertical sweeps also
+      // read the never-written horizontal ones
+      for (int y = 0; y < H; ++y)
+        for (int c = 0; c < L; ++c) {
+          g_msgs[S.msg(n, LEFT, y, 0) + c] += in_grad[S.msg(n, LEFT, y, 0) + c] +
+                                             saved[S.msg(n, UP, y, 0) + c] + saved[S.msg(n, DOWN, y, 0) + c];
+          g_msgs[S.msg(n, RIGHT, y, W - 1) + c] += in_grad[S.msg(n, RIGHT, y, W - 1) + c] +
+                                                  saved[S.msg(n, UP, y, W - 1) + c] +
+                                                  saved[S.msg(n, DOWN, y, W - 1) + c];
+        }
+      for (int x = 0; x < W; ++x)
+        for (int c = 0; c < L; ++c) {
+          g_msgs[S.msg(n, UP, 0, x) + c] += in_grad[S.msg(n, UP, 0, x) + c];
+          g_msgs[S.msg(n, DOWN, H - 1, x) + c] += in_grad[S.msg(n, DOWN, H - 1, x) + c];
+        }
+    }
   }
+}
+
+void lbp_backward_ref(int variant, const float* jump, const float* edge, const float* in_grad,
+                      const float* msgs, const float* argmin, const float* scale, double* g_cost,
+                      double* g_jump, double* g_edge, double* g_msgs, int B, int H, int W, int L,
+                      int Lv, int jb, int eb, int threads) {
+  lbp_backward_t<float>(variant, false, jump, edge, in_grad, msgs, argmin, scale, g_cost, g_jump, g_edge,
+                        g_msgs, B, H, W, L, Lv, jb, eb, threads);
 }
 
 // ---------------------------------------------------------------------------
@@ -578,6 +650,27 @@ void oracle_lbp_backward_ref(int variant, const float* jump, const float* edge,
                              int Lv, int jump_batch, int edge_batch, int threads) {
   lbp_backward_ref(variant, jump, edge, in_grad, messages, argmin, scale, grad_cost, grad_jump,
                    grad_edge, grad_messages, B, H, W, L, Lv, jump_batch, edge_batch, threads);
+}
+
+// Exact adjoint (see lbp_backward_t) for float and double forward results.
+void oracle_lbp_backward_exact_f32(int variant, const float* jump, const float* edge,
+                                   const float* in_grad, const float* messages, const float* argmin,
+                                   const float* scale, double* grad_cost, double* grad_jump,
+                                   double* grad_edge, double* grad_messages, int B, int H, int W,
+                                   int L, int Lv, int jump_batch, int edge_batch, int threads) {
+  lbp_backward_t<float>(variant, true, jump, edge, in_grad, messages, argmin, scale, grad_cost,
+                        grad_jump, grad_edge, grad_messages, B, H, W, L, Lv, jump_batch, edge_batch,
+                        threads);
+}
+
+void oracle_lbp_backward_exact_f64(int variant, const double* jump, const double* edge,
+                                   const double* in_grad, const double* messages, const float* argmin,
+                                   const double* scale, double* grad_cost, double* grad_jump,
+                                   double* grad_edge, double* grad_messages, int B, int H, int W,
+                                   int L, int Lv, int jump_batch, int edge_batch, int threads) {
+  lbp_backward_t<double>(variant, true, jump, edge, in_grad, messages, argmin, scale, grad_cost,
+                         grad_jump, grad_edge, grad_messages, B, H, W, L, Lv, jump_batch, edge_batch,
+                         threads);
 }
 
 void oracle_sad_forward(const float* f0, const float* f1, float* out, int B, int C, int H, int W,

@@ -110,6 +110,34 @@ def lbp_backward_ref(variant, jump, edge, in_grad, messages, argmin, scale, *, t
     return gc, gj, ge, gm
 
 
+def lbp_backward_exact(variant, jump, edge, in_grad, messages, argmin, scale, *, fp64=False, threads=0):
+    """Exact adjoint of one pass (the reverse-mode derivative of the forward
+    as written), from that pass's outputs (messages, argmin, scale) in float
+    (fp64=False) or double (fp64=True).  Returns (grad_cost, grad_jump,
+    grad_edge, grad_messages) as float64, grad_messages with respect to the
+    pass's input messages."""
+    B, _, H, W, L = messages.shape
+    if variant == VAR_STEREO:
+        Lv, jb = jump.shape[2], jump.shape[0]
+        gj = np.zeros((B, 4, Lv, H, W))
+    elif variant == VAR_SEM_GLOBAL:
+        Lv, jb = 0, 1
+        gj = np.zeros((B, 4, L, L))
+    else:
+        Lv, jb = 0, 1
+        gj = np.zeros((4, H, W, L, L))
+    eb = edge.shape[0]
+    gc = np.zeros((B, H, W, L))
+    ge = np.zeros((B, 4, H, W))
+    gm = np.zeros((B, 4, H, W, L))
+    conv = _f64 if fp64 else _f32
+    fn = lib().oracle_lbp_backward_exact_f64 if fp64 else lib().oracle_lbp_backward_exact_f32
+    fn(ctypes.c_int(variant), _p(conv(jump)), _p(conv(edge)), _p(conv(in_grad)), _p(conv(messages)),
+       _p(_f32(argmin)), _p(conv(scale)), _p(gc), _p(gj), _p(ge), _p(gm),
+       *[ctypes.c_int(v) for v in (B, H, W, L, Lv, jb, eb, threads)])
+    return gc, gj, ge, gm
+
+
 def sad_forward(f0, f1, min_disp, max_disp, step=1.0, *, all_batches=True, threads=0):
     B, C, H, W = f0.shape
     D = int((max_disp - min_disp + 1) / step)
