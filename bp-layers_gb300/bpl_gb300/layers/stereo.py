@@ -70,27 +70,36 @@ def unpack_affinity_grad(grad_taps):
 
 
 class LBPMinSumFunction(torch.autograd.Function):
-    """One LBP pass with the reference adjoint
-    (message_passing_op_cuda.py:22-93).  forward(cost, edge, messages, delta,
-    affinities, offset) -> messages (updated in place, like the reference)."""
+    """One LBP pass (message_passing_op_cuda.py:22-93).  forward(cost, edge,
+    messages, delta, affinities, offset[, adjoint]) -> messages (updated in
+    place, like the reference).
+
+    adjoint "reference": the reference's backward, which uses the messages
+    as they are when backward runs (the last pass's, for every pass) and
+    returns in_grad as the message gradient.  adjoint "exact": the
+    derivative of the forward; each pass keeps a copy of its own output
+    messages and returns the gradient with respect to its input messages,
+    so chained passes differentiate exactly."""
 
     @staticmethod
-    def forward(ctx, cost, edge, messages, delta, affinities, offset):
+    def forward(ctx, cost, edge, messages, delta, affinities, offset, adjoint="reference"):
         taps = pack_affinities(affinities, offset)
         L = cost.shape[-1]
         am_dtype = torch.uint8 if L <= 256 else torch.int16
         messages, argmin, scale = ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta),
                                                   argmin_dtype=am_dtype)
-        ctx.save_for_backward(cost, taps, edge, messages, argmin, scale)
+        ctx.adjoint = adjoint
+        own = messages.clone() if adjoint == "exact" else messages
+        ctx.save_for_backward(cost, taps, edge, own, argmin, scale)
         return messages
 
     @staticmethod
     def backward(ctx, in_grad):
         cost, taps, edge, messages, argmin, scale = ctx.saved_tensors
         gc, gtaps, ge, gm = ops.lbp_backward(ops.LBP_STEREO, taps, edge, in_grad.contiguous(), messages, argmin,
-                                             scale, copy_grad_messages=False)
+                                             scale, copy_grad_messages=False, mode=ctx.adjoint)
         g_aff, g_off = unpack_affinity_grad(gtaps)
-        return gc, ge, gm, None, g_aff, g_off
+        return gc, ge, gm, None, g_aff, g_off, None
 
 
 class LBPMinSumFunctionF16(torch.autograd.Function):
@@ -145,7 +154,7 @@ class MessagePassing(nn.Module):
         elif value_L1 > value_L2:
             raise ValueError("L1 must be smaller than or equal L2!")
 
-    def __init__(self, device, max_iter, num_labels, delta, mode="min-sum", storage="fp32"):
+    def __init__(self, device, max_iter, num_labels, delta, mode="min-sum", storage="fp32", adjoint="reference"):
         super().__init__()
         self.device = device
         self.max_iter = max_iter
@@ -153,6 +162,11 @@ class MessagePassing(nn.Module):
             raise ValueError("Unknown message parsing mode " + mode)
         if storage not in ("fp32", "fp16"):
             raise ValueError("storage must be fp32 or fp16")
+        if adjoint not in ("reference", "exact"):
+            raise ValueError("adjoint must be reference or exact")
+        if adjoint == "exact" and storage != "fp32":
+            raise ValueError("the exact adjoint runs with fp32 storage")
+        self.adjoint = adjoint
         self.mode = mode
         self.storage = storage
         self._L1 = nn.Parameter(torch.tensor(0.1, device=device), requires_grad=True)
@@ -193,7 +207,8 @@ class MessagePassing(nn.Module):
             beliefs = messages[..., :C].float().sum(dim=1) + cost
             return self.softmin.forward(beliefs), messages
         for _ in range(self.max_iter):
-            messages = LBPMinSumFunction.apply(cost, edge_weights, messages, self.delta, affinities, offset)
+            messages = LBPMinSumFunction.apply(cost, edge_weights, messages, self.delta, affinities, offset,
+                                               self.adjoint)
         beliefs = messages.sum(dim=1) + cost
         beliefs = self.softmin.forward(beliefs)
         return beliefs, messages

@@ -92,14 +92,19 @@ def lbp_backward_workspace_bytes(B: int, H: int, W: int, L: int) -> int:
 
 def lbp_backward(variant: int, jump, edge: torch.Tensor, in_grad: torch.Tensor, messages: torch.Tensor,
                  argmin: torch.Tensor, scale: torch.Tensor, workspace: torch.Tensor | None = None,
-                 copy_grad_messages: bool = True):
-    """Reference adjoint of one LBP pass.
+                 copy_grad_messages: bool = True, mode: str = "reference"):
+    """Adjoint of one LBP pass.
 
-    Returns (grad_cost, grad_jump, grad_edge, grad_messages).  grad_messages
-    is in_grad (copied unless copy_grad_messages=False), grad_edge is None
-    for the pixel-pairwise variant.  `workspace` (uint8, at least
-    lbp_backward_workspace_bytes) may be passed to avoid allocating it.
+    Returns (grad_cost, grad_jump, grad_edge, grad_messages).  mode
+    "reference": the reference's adjoint, grad_messages is in_grad (copied
+    unless copy_grad_messages=False); mode "exact": grad_messages is the
+    gradient with respect to the pass's input messages (the other gradients
+    are the same in both modes).  grad_edge is None for the pixel-pairwise
+    variant.  `workspace` (uint8, at least lbp_backward_workspace_bytes) may
+    be passed to avoid allocating it.
     """
+    if mode not in ("reference", "exact"):
+        raise BplError(f"unknown adjoint mode {mode!r}")
     _check_input("in_grad", in_grad, dim=5)
     _check_input("messages", messages, dim=5)
     _check_input("scale", scale, dim=4)
@@ -127,6 +132,15 @@ def lbp_backward(variant: int, jump, edge: torch.Tensor, in_grad: torch.Tensor, 
     need = lbp_backward_workspace_bytes(B, H, W, L)
     if workspace is None or workspace.numel() * workspace.element_size() < need:
         workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    if mode == "exact":
+        grad_messages = torch.empty_like(messages)
+        st = _timed("lbp_backward", lambda: lib().bpl_lbp_backward_exact(
+            variant, _ptr(jump) if variant != LBP_SEM_PIXEL else None, _ptr(edge), _ptr(in_grad),
+            _ptr(messages), _ptr(argmin), kind, _ptr(scale), _ptr(grad_cost), _ptr(grad_jump),
+            _ptr(grad_edge), _ptr(grad_messages), _ptr(workspace), workspace.numel() * workspace.element_size(),
+            B, H, W, L, Lv, jb, edge.shape[0], _stream(messages)))
+        check(st, "bpl_lbp_backward_exact")
+        return grad_cost, grad_jump, grad_edge, grad_messages
     st = _timed("lbp_backward", lambda: lib().bpl_lbp_backward(
         variant, _ptr(jump) if variant != LBP_SEM_PIXEL else None, _ptr(edge), _ptr(in_grad),
         _ptr(messages), _ptr(argmin), kind, _ptr(scale), _ptr(grad_cost), _ptr(grad_jump),

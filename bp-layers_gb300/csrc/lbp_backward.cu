@@ -1,5 +1,7 @@
 // C-ABI entry of the LBP reference adjoint (argument checks, output
 // zero-fill, dispatch).
+#include <algorithm>
+
 #include "lbp_backward.cuh"
 
 using namespace bpl;
@@ -13,10 +15,48 @@ namespace {
 
 // storage: 0 = float messages (reference layout), 1 = half messages with the
 // label axis padded to Lp = L rounded up to 8
+// Completes the exact message gradient (the pass's input messages) from
+// what the horizontal adjoint sweeps left in gmsg: slot UP holds the h
+// gradients of the horizontal senders (they read the input vertical
+// messages at every pixel), slots LEFT at x=0 / RIGHT at x=W-1 the chain
+// inputs' gradients.  Adds, where a slot is never written by the pass (its
+// input passes through and is read by the sweeps there): the upstream
+// gradient, and the vertical sweeps' h gradients (saved accumulators) --
+// UP at y=0 (the DOWN sweep's chain input), DOWN at y=H-1, and both for the
+// horizontal slots at the image's left and right columns.
+__global__ void assemble_message_grad_kernel(const float* in_grad, const float* saved, float* gmsg, int B, int H,
+                                             int W, int L, int Ls) {
+  const int64_t HW = static_cast<int64_t>(H) * W;
+  const int64_t HWL = HW * Ls;
+  const int64_t total = static_cast<int64_t>(B) * HW * Ls;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int t = static_cast<int>(i % Ls);
+    const int64_t pix = i / Ls;
+    const int n = static_cast<int>(pix / HW);
+    const int64_t pin = pix % HW;
+    const int y = static_cast<int>(pin / W), x = static_cast<int>(pin % W);
+    float* gm = gmsg + static_cast<int64_t>(n) * 4 * HWL + pin * Ls + t;
+    const float* gi = in_grad + static_cast<int64_t>(n) * 4 * HWL + pin * Ls + t;
+    if (t >= L) {
+      gm[LEFT * HWL] = gm[RIGHT * HWL] = gm[UP * HWL] = gm[DOWN * HWL] = 0.0f;
+      continue;
+    }
+    const float sU = saved[(static_cast<int64_t>(n) * 2 + 0) * HWL + pin * Ls + t];
+    const float sD = saved[(static_cast<int64_t>(n) * 2 + 1) * HWL + pin * Ls + t];
+    const float gh = gm[UP * HWL];
+    gm[UP * HWL] = gh + ((y == 0) ? gi[UP * HWL] + sU : 0.0f);
+    gm[DOWN * HWL] = gh + ((y == H - 1) ? gi[DOWN * HWL] + sD : 0.0f);
+    gm[LEFT * HWL] = (x == 0) ? gm[LEFT * HWL] + gi[LEFT * HWL] + sU + sD : 0.0f;
+    gm[RIGHT * HWL] = (x == W - 1) ? gm[RIGHT * HWL] + gi[RIGHT * HWL] + sU + sD : 0.0f;
+  }
+}
+
 int lbp_backward_impl(int storage, int variant, const float* jump, const float* edge, const void* in_grad,
                       const void* messages, const void* argmin, int argmin_kind, const float* scale,
                       float* grad_cost, float* grad_jump, float* grad_edge, void* workspace, size_t workspace_bytes,
-                      int B, int H, int W, int L, int Lv, int jump_batch, int edge_batch, void* stream) {
+                      int B, int H, int W, int L, int Lv, int jump_batch, int edge_batch, void* stream,
+                      float* grad_messages = nullptr) {
   BPL_REQUIRE(variant >= 0 && variant <= 2, "lbp_backward: unknown variant %d", variant);
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1, "lbp_backward: bad shape B=%d H=%d W=%d", B, H, W);
   BPL_REQUIRE(H <= 65535 && W <= 65535, "lbp_backward: H and W must be <= 65535");
@@ -47,6 +87,8 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   BPL_CUDA_TRY(cudaMemsetAsync(grad_jump, 0, sizeof(float) * gj_elems, s), "lbp_backward: memset");
   if (grad_edge)
     BPL_CUDA_TRY(cudaMemsetAsync(grad_edge, 0, sizeof(float) * edge_batch * 4 * HW, s), "lbp_backward: memset");
+  if (grad_messages)
+    BPL_CUDA_TRY(cudaMemsetAsync(grad_messages, 0, sizeof(float) * B * 4 * HW * Ls, s), "lbp_backward: memset");
 
   BwdArgs a{};
   a.jump = jump;
@@ -59,6 +101,7 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   a.grad_jump = grad_jump;
   a.grad_edge = grad_edge;
   a.saved = static_cast<float*>(workspace);
+  a.gmsg = grad_messages;
   a.B = B;
   a.H = H;
   a.W = W;
@@ -80,11 +123,19 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   a.ns = 0;  // rows are prefetched into registers: no shared-memory ring
   if (storage == 1)
     return (variant == BPL_LBP_STEREO) ? lbp_backward_stereo_f16(a, s) : lbp_backward_sem_pixel_f16(a, s);
+  int st;
   switch (variant) {
-    case BPL_LBP_STEREO: return lbp_backward_stereo(a, s);
-    case BPL_LBP_SEM_GLOBAL: return lbp_backward_sem_global(a, s);
-    default: return lbp_backward_sem_pixel(a, s);
+    case BPL_LBP_STEREO: st = lbp_backward_stereo(a, s); break;
+    case BPL_LBP_SEM_GLOBAL: st = lbp_backward_sem_global(a, s); break;
+    default: st = lbp_backward_sem_pixel(a, s); break;
   }
+  if (st != BPL_OK || grad_messages == nullptr) return st;
+  const int64_t total = static_cast<int64_t>(B) * HW * Ls;
+  const int blocks = static_cast<int>(std::min<int64_t>((total + 255) / 256, 8 * 152 * 8));
+  assemble_message_grad_kernel<<<blocks, 256, 0, s>>>(static_cast<const float*>(in_grad), a.saved, grad_messages, B,
+                                                     H, W, L, Ls);
+  BPL_CUDA_TRY(cudaGetLastError(), "lbp_backward: message-gradient launch");
+  return BPL_OK;
 }
 
 }  // namespace
@@ -97,6 +148,17 @@ extern "C" int bpl_lbp_backward(int variant, const float* jump, const float* edg
   return lbp_backward_impl(0, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
                            stream);
+}
+
+extern "C" int bpl_lbp_backward_exact(int variant, const float* jump, const float* edge, const float* in_grad,
+                                      const float* messages, const void* argmin, int argmin_kind,
+                                      const float* scale, float* grad_cost, float* grad_jump, float* grad_edge,
+                                      float* grad_messages, void* workspace, size_t workspace_bytes, int B, int H,
+                                      int W, int L, int Lv, int jump_batch, int edge_batch, void* stream) {
+  BPL_REQUIRE(grad_messages, "lbp_backward_exact: null grad_messages");
+  return lbp_backward_impl(0, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
+                           grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
+                           stream, grad_messages);
 }
 
 extern "C" int bpl_lbp_backward_f16(int variant, const float* jump, const float* edge, const void* in_grad,

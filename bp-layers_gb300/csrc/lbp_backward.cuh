@@ -49,6 +49,12 @@ struct BwdArgs {
   float* grad_jump;
   float* grad_edge;
   float* saved;  // workspace (B,2,H,W,L): slot 0 = UP chain, slot 1 = DOWN chain
+  // exact adjoint only (else null): (B,4,H,W,Ls) float message gradient.
+  // The horizontal sweeps add each sender's h gradient to slot UP (the
+  // vertical input messages they read) and write it at their first sender
+  // to their own slot (the chain input); bpl_lbp_assemble_message_grad
+  // completes it.
+  float* gmsg;
   int B, H, W, L, Lv, jb, eb;
   int Ls;
   int argmin_kind;
@@ -463,6 +469,11 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
       }
       if (t < L && v != 0.0f) atomicAdd(gc + t, v);
       if (!CROSS && t < L) saved_out[static_cast<int64_t>(p) * Ls + t] = accH[kk];
+      if (CROSS && a.gmsg != nullptr && t < L) {
+        float* gm = a.gmsg + static_cast<int64_t>(n) * 4 * HWL;
+        if (v != 0.0f) atomicAdd(gm + UP * HWL + static_cast<int64_t>(p) * Ls + t, v);
+        if (k == nsteps - 1) gm[db * HWL + static_cast<int64_t>(p) * Ls + t] = v;
+      }
     }
 
     if (j == 31 || k == nsteps - 1) {

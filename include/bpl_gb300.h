@@ -141,6 +141,28 @@ int bpl_lbp_backward(int variant, const float* jump, const float* edge, const fl
                      size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
                      int edge_batch, void* stream);
 
+/*
+ * Exact adjoint of one LBP pass (FP32 storage).  No counterpart in the
+ * reference, whose adjoint (bpl_lbp_backward) returns in_grad as the message
+ * gradient; the cost, jump and edge gradients are the reference adjoint's
+ * (the reference carries the vertical sweeps' accumulators without the
+ * normalisation's Jacobian, which is exact because every vector that
+ * Jacobian's transpose produces sums to zero).  grad_messages (B,4,H,W,L)
+ * receives the gradient with respect to the pass's input messages: the
+ * vertical messages read by the horizontal sweeps at every pixel, the chain
+ * inputs at each sweep's first sender, and, for the slots the pass never
+ * writes (LEFT at x=0, RIGHT at x=W-1, UP at y=0, DOWN at y=H-1), the
+ * upstream gradient passing through plus the vertical sweeps' reads.  With
+ * it the gradient of several chained passes is the derivative of the
+ * forward (checked against central finite differences in FP64 on the
+ * oracle).  Other arguments as bpl_lbp_backward.
+ */
+int bpl_lbp_backward_exact(int variant, const float* jump, const float* edge, const float* in_grad,
+                           const float* messages, const void* argmin, int argmin_kind, const float* scale,
+                           float* grad_cost, float* grad_jump, float* grad_edge, float* grad_messages,
+                           void* workspace, size_t workspace_bytes, int B, int H, int W, int L, int Lv,
+                           int jump_batch, int edge_batch, void* stream);
+
 /* Disparity count D of the SAD volume: (int)((max_disp - min_disp + 1) / step)
  * (ops/sad/src/stereo_sad_kernel.cu:122); -1 for a non-positive step. */
 int bpl_sad_volume_depth(int min_disp, int max_disp, float step);

@@ -1,0 +1,85 @@
+"""Exact adjoint on the GPU (bpl_lbp_backward_exact) against the oracle's
+exact adjoint (whose derivative is checked against FP64 central finite
+differences in test_exact_adjoint.py), for one pass and through the
+MessagePassing layer with adjoint="exact"."""
+import numpy as np
+import pytest
+
+import cases
+import oracle
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.mark.parametrize("shape", [(2, 12, 20, 16), (1, 17, 23, 64)], ids=["b2_l16", "b1_l64"])
+def test_exact_backward_single_pass(shape):
+    from bpl_gb300 import ops
+    dev = torch.device("cuda:0")
+    B, H, W, L = shape
+    g = cases.rng(31)
+    cost = cases.random_cost(g, B, H, W, L)
+    edge = cases.edge_weights(g, B, H, W)
+    jump = cases.stereo_taps(B, H, W, 0.1, 0.5)
+    m_in = g.normal(0, 0.3, size=(B, 4, H, W, L)).astype(np.float32)
+    G = g.normal(0, 1, size=(B, 4, H, W, L)).astype(np.float32)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    m, am, sc = ops.lbp_forward(0, t(cost), t(jump), t(edge), t(m_in), 3, argmin_dtype=torch.uint8)
+    gc, gj, ge, gm = ops.lbp_backward(0, t(jump), t(edge), t(G), m, am, sc, mode="exact")
+    ref = oracle.lbp_backward_exact(0, jump, edge, G, m.cpu().numpy(), am.cpu().numpy().astype(np.float32),
+                                    sc.cpu().numpy())
+    for name, got, want in zip(("cost", "jump", "edge", "messages"), (gc, gj, ge, gm), ref):
+        got = got.cpu().numpy()
+        err = np.abs(got - want).max()
+        assert err <= 2e-4 * max(1.0, np.abs(want).max()), (name, err, np.abs(want).max())
+
+
+def _softmin(x):
+    x = -x.astype(np.float64)
+    x -= x.max(-1, keepdims=True)
+    e = np.exp(x)
+    return e / e.sum(-1, keepdims=True)
+
+
+def test_message_passing_exact_adjoint_through_iterations():
+    from bpl_gb300.layers.stereo import MessagePassing
+    dev = torch.device("cuda:0")
+    g = cases.rng(13)
+    B, H, W, L, iters = 1, 14, 22, 32, 3
+    prob = cases.softmax_np(g.normal(0, 2, size=(B, H, W, L)).astype(np.float32))
+    edge = cases.edge_weights(g, B, H, W)
+    up = g.normal(0, 1, size=(B, H, W, L)).astype(np.float32)
+    mp = MessagePassing(dev, iters, L, 3, adjoint="exact")
+    with torch.no_grad():
+        mp._L1.fill_(0.1)
+        mp._L2.fill_(0.5)
+    p = torch.from_numpy(prob).to(dev).requires_grad_(True)
+    m0 = torch.zeros((B, 4, H, W, L), device=dev, requires_grad=True)
+    beliefs, _ = mp(p, torch.from_numpy(edge).to(dev), None, None, m0)
+    beliefs.backward(torch.from_numpy(up).to(dev))
+
+    # oracle: the same passes, then the exact adjoint chained backwards
+    cost = -prob
+    jump = cases.stereo_taps(B, H, W, 0.1, 0.5)
+    m = np.zeros((B, 4, H, W, L), np.float32)
+    per_it = []
+    for _ in range(iters):
+        m, am, sc = oracle.lbp_forward(0, cost, jump, edge, m, 3)
+        per_it.append((m.copy(), am.copy(), sc.copy()))
+    bz = _softmin(m.sum(1) + cost)
+    g_sum = -(bz * (up - (up * bz).sum(-1, keepdims=True)))
+    G = np.broadcast_to(g_sum[:, None], (B, 4, H, W, L)).astype(np.float64)
+    gcost = g_sum.copy()
+    gL1 = gL2 = 0.0
+    for mk, amk, sck in reversed(per_it):
+        gc, gj, _, gm = oracle.lbp_backward_exact(0, jump, edge, G, mk, amk, sck)
+        gcost += gc
+        gL1 += gj[:, :, 2].sum() + gj[:, :, 4].sum()
+        gL2 += gj[:, :, 1].sum() + gj[:, :, 5].sum()
+        G = gm
+    got = p.grad.detach().cpu().numpy()
+    np.testing.assert_allclose(got, -gcost, atol=2e-4 * np.abs(gcost).max())
+    assert abs(mp._L1.grad.item() - gL1) <= 2e-4 * max(abs(gL1), 1.0)
+    assert abs(mp._L2.grad.item() - gL2) <= 2e-4 * max(abs(gL2), 1.0)
+    # the initial messages' gradient is the first pass's input-message gradient
+    np.testing.assert_allclose(m0.grad.detach().cpu().numpy(), G, atol=2e-4 * max(1.0, np.abs(G).max()))
