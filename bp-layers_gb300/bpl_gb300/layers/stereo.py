@@ -129,6 +129,49 @@ class LBPMinSumFunctionF16(torch.autograd.Function):
         return gc[..., :ctx.L], None, ge, in_grad, None, g_aff, g_off
 
 
+class LBPMinSumLoop(torch.autograd.Function):
+    """`iters` LBP passes run in place with the reference adjoint, as one
+    autograd node.  The reference's per-pass nodes
+    (message_passing_op_cuda.py:161-168) each read the final, overwritten
+    messages in backward and pass in_grad through as the message gradient,
+    so their adjoints are independent of each other: here they run as one
+    launch (bpl_lbp_backward_passes), which triples the scanlines of the
+    latency-bound horizontal sweeps at 3 iterations.  Gradients equal the
+    chained per-pass nodes'.  FP32 or FP16 storage (cost_h and messages
+    half with the padded label axis)."""
+
+    @staticmethod
+    def forward(ctx, cost, cost_h, edge, messages, delta, affinities, offset, iters):
+        taps = pack_affinities(affinities, offset)
+        half = messages.dtype == torch.float16
+        L = cost.shape[-1]
+        B, _, H, W, Ls = messages.shape
+        am_dtype = torch.uint8 if L <= 256 else torch.int16
+        argmins = torch.empty((iters, B, 4, H, W, Ls), dtype=am_dtype, device=cost.device)
+        scales = torch.empty((iters, B, 4, H, W), dtype=torch.float32, device=cost.device)
+        for k in range(iters):
+            if half:
+                ops.lbp_forward_f16(ops.LBP_STEREO, cost_h, taps, edge, messages, int(delta), L,
+                                    argmin_dtype=am_dtype, argmin=argmins[k], scale=scales[k])
+            else:
+                ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta), argmin_dtype=am_dtype,
+                                argmin=argmins[k], scale=scales[k])
+        ctx.save_for_backward(taps, edge, messages, argmins, scales)
+        ctx.L = L
+        ctx.half = half
+        return messages
+
+    @staticmethod
+    def backward(ctx, in_grad):
+        taps, edge, messages, argmins, scales = ctx.saved_tensors
+        gc, gtaps, ge = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, in_grad.contiguous(), messages,
+                                                argmins, scales, L=ctx.L)
+        g_aff, g_off = unpack_affinity_grad(gtaps)
+        if ctx.half:
+            gc = gc[..., :ctx.L]
+        return gc, None, ge, in_grad, None, g_aff, g_off, None
+
+
 class MessagePassing(nn.Module):
     """message_passing_op_cuda.py:95-177.  storage="fp16" keeps the cost
     volume and the messages in half precision (label axis padded to a
@@ -201,14 +244,17 @@ class MessagePassing(nn.Module):
                 if messages is not None:
                     m[..., :C] = messages.detach()
                 messages = m.requires_grad_(True)
-            for _ in range(self.max_iter):
-                messages = LBPMinSumFunctionF16.apply(cost, cost_h, edge_weights, messages, self.delta, affinities,
-                                                      offset)
+            messages = LBPMinSumLoop.apply(cost, cost_h, edge_weights, messages, self.delta, affinities, offset,
+                                           self.max_iter)
             beliefs = messages[..., :C].float().sum(dim=1) + cost
             return self.softmin.forward(beliefs), messages
-        for _ in range(self.max_iter):
-            messages = LBPMinSumFunction.apply(cost, edge_weights, messages, self.delta, affinities, offset,
-                                               self.adjoint)
+        if self.adjoint == "reference":
+            messages = LBPMinSumLoop.apply(cost, None, edge_weights, messages, self.delta, affinities, offset,
+                                           self.max_iter)
+        else:
+            for _ in range(self.max_iter):
+                messages = LBPMinSumFunction.apply(cost, edge_weights, messages, self.delta, affinities, offset,
+                                                   self.adjoint)
         beliefs = messages.sum(dim=1) + cost
         beliefs = self.softmin.forward(beliefs)
         return beliefs, messages

@@ -362,3 +362,56 @@ def lbp_backward_f16(variant: int, jump, edge: torch.Tensor, in_grad_h: torch.Te
         workspace.numel() * workspace.element_size(), B, H, W, L, Lv, jb, edge.shape[0], _stream(messages_h)))
     check(st, "bpl_lbp_backward_f16")
     return grad_cost, grad_jump, grad_edge
+
+
+def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.Tensor, messages: torch.Tensor,
+                        argmins: torch.Tensor, scales: torch.Tensor, L: int | None = None,
+                        workspace: torch.Tensor | None = None):
+    """Reference adjoint of P passes run in place on one messages tensor,
+    in one launch: argmins (P,B,4,H,W,Ls) and scales (P,B,4,H,W) stacked in
+    pass order; in_grad and messages shared (the reference's backward of each
+    pass reads the final messages and passes in_grad through).  FP32
+    (messages float32) or FP16 storage (messages half, padded label axis,
+    L given).  Returns (grad_cost, grad_jump, grad_edge) summed over the
+    passes; the message gradient is in_grad."""
+    half = messages.dtype == torch.float16
+    _check_input("in_grad", in_grad, dtype=messages.dtype, dim=5)
+    _check_input("messages", messages, dtype=None, dim=5)
+    _check_input("argmins", argmins, dtype=None, dim=6)
+    _check_input("scales", scales, dim=5)
+    _check_input("edge", edge, dim=4)
+    B, _, H, W, Ls = messages.shape
+    P = argmins.shape[0]
+    if L is None:
+        L = Ls
+    if tuple(argmins.shape) != (P, B, 4, H, W, Ls) or tuple(scales.shape) != (P, B, 4, H, W):
+        raise BplError("argmins/scales must be stacked (P,B,4,H,W,Ls) / (P,B,4,H,W)")
+    if half and Ls != padded_labels(L):
+        raise BplError("FP16 messages must have the padded label axis")
+    kind = _ARGMIN_KIND.get(argmins.dtype)
+    if kind is None:
+        raise BplError(f"argmin dtype {argmins.dtype} not supported")
+    dev = messages.device
+    Lv, jb = 0, 1
+    if variant == LBP_STEREO:
+        _check_input("jump", jump, dim=5)
+        Lv, jb = jump.shape[2], jump.shape[0]
+        grad_jump = torch.empty((jb, 4, Lv, H, W), dtype=torch.float32, device=dev)
+    elif variant == LBP_SEM_GLOBAL:
+        _check_input("jump", jump, dim=4)
+        grad_jump = torch.empty((B, 4, L, L), dtype=torch.float32, device=dev)
+    else:
+        grad_jump = torch.empty((4, H, W, L, L), dtype=torch.float32, device=dev)
+    grad_cost = torch.empty((B, H, W, Ls), dtype=torch.float32, device=dev)
+    grad_edge = None if variant == LBP_SEM_PIXEL else torch.empty(tuple(edge.shape), dtype=torch.float32, device=dev)
+    need = P * lbp_backward_workspace_bytes(B, H, W, Ls)
+    if workspace is None or workspace.numel() * workspace.element_size() < need:
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    fn = lib().bpl_lbp_backward_passes_f16 if half else lib().bpl_lbp_backward_passes
+    name = "lbp_backward_f16" if half else "lbp_backward"
+    st = _timed(name, lambda: fn(
+        variant, _ptr(jump) if variant != LBP_SEM_PIXEL else None, _ptr(edge), _ptr(in_grad), _ptr(messages),
+        _ptr(argmins), kind, _ptr(scales), _ptr(grad_cost), _ptr(grad_jump), _ptr(grad_edge), _ptr(workspace),
+        workspace.numel() * workspace.element_size(), B, H, W, L, Lv, jb, edge.shape[0], P, _stream(messages)))
+    check(st, "bpl_lbp_backward_passes")
+    return grad_cost, grad_jump, grad_edge

@@ -56,7 +56,7 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
                       const void* messages, const void* argmin, int argmin_kind, const float* scale,
                       float* grad_cost, float* grad_jump, float* grad_edge, void* workspace, size_t workspace_bytes,
                       int B, int H, int W, int L, int Lv, int jump_batch, int edge_batch, void* stream,
-                      float* grad_messages = nullptr) {
+                      float* grad_messages = nullptr, int reps = 1) {
   BPL_REQUIRE(variant >= 0 && variant <= 2, "lbp_backward: unknown variant %d", variant);
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1, "lbp_backward: bad shape B=%d H=%d W=%d", B, H, W);
   BPL_REQUIRE(H <= 65535 && W <= 65535, "lbp_backward: H and W must be <= 65535");
@@ -67,8 +67,9 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   BPL_REQUIRE(argmin_kind >= BPL_ARGMIN_F32 && argmin_kind <= BPL_ARGMIN_U16, "lbp_backward: bad argmin kind");
   BPL_REQUIRE(edge_batch == 1 || edge_batch == B, "lbp_backward: edge batch %d must be 1 or B", edge_batch);
   const int Ls = (storage == 0) ? L : ((L + 7) & ~7);
-  BPL_REQUIRE(workspace && workspace_bytes >= bpl_lbp_backward_workspace_size(B, H, W, Ls),
-              "lbp_backward: workspace of %zu bytes needed", bpl_lbp_backward_workspace_size(B, H, W, Ls));
+  BPL_REQUIRE(reps >= 1 && (reps == 1 || grad_messages == nullptr), "lbp_backward: bad pass count %d", reps);
+  BPL_REQUIRE(workspace && workspace_bytes >= reps * bpl_lbp_backward_workspace_size(B, H, W, Ls),
+              "lbp_backward: workspace of %zu bytes needed", reps * bpl_lbp_backward_workspace_size(B, H, W, Ls));
   if (variant == BPL_LBP_STEREO) {
     BPL_REQUIRE(Lv >= 2 && Lv <= 16, "lbp_backward: Lv=%d outside [2, 16]", Lv);
     BPL_REQUIRE(jump_batch == 1 || jump_batch == B, "lbp_backward: jump batch %d must be 1 or B", jump_batch);
@@ -102,6 +103,7 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   a.grad_edge = grad_edge;
   a.saved = static_cast<float*>(workspace);
   a.gmsg = grad_messages;
+  a.reps = reps;
   a.B = B;
   a.H = H;
   a.W = W;
@@ -159,6 +161,27 @@ extern "C" int bpl_lbp_backward_exact(int variant, const float* jump, const floa
   return lbp_backward_impl(0, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
                            stream, grad_messages);
+}
+
+extern "C" int bpl_lbp_backward_passes(int variant, const float* jump, const float* edge, const float* in_grad,
+                                       const float* messages, const void* argmin, int argmin_kind,
+                                       const float* scale, float* grad_cost, float* grad_jump, float* grad_edge,
+                                       void* workspace, size_t workspace_bytes, int B, int H, int W, int L, int Lv,
+                                       int jump_batch, int edge_batch, int passes, void* stream) {
+  return lbp_backward_impl(0, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
+                           grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
+                           stream, nullptr, passes);
+}
+
+extern "C" int bpl_lbp_backward_passes_f16(int variant, const float* jump, const float* edge, const void* in_grad,
+                                           const void* messages, const void* argmin, int argmin_kind,
+                                           const float* scale, float* grad_cost, float* grad_jump,
+                                           float* grad_edge, void* workspace, size_t workspace_bytes, int B, int H,
+                                           int W, int L, int Lv, int jump_batch, int edge_batch, int passes,
+                                           void* stream) {
+  return lbp_backward_impl(1, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
+                           grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
+                           stream, nullptr, passes);
 }
 
 extern "C" int bpl_lbp_backward_f16(int variant, const float* jump, const float* edge, const void* in_grad,

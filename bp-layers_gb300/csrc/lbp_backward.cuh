@@ -56,6 +56,11 @@ struct BwdArgs {
   // completes it.
   float* gmsg;
   int B, H, W, L, Lv, jb, eb;
+  // passes sharing messages and in_grad (the reference adjoint of an
+  // in-place iteration loop): argmin, scale and the workspace are stacked
+  // (reps, B, ...); the chains of all passes run in one launch and their
+  // gradients accumulate into the same outputs
+  int reps;
   int Ls;
   int argmin_kind;
   int phase;  // 0: DOWN+UP over columns, 1: LEFT+RIGHT over rows
@@ -146,12 +151,12 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
   const int64_t HWL = HW * Ls;
   // chain: sender of step k is pin0 + k*dpin (pixel index within the image),
   // its receiver is dq further
-  int n, db, pin0, dpin, dq, nsteps;
+  int n, v, db, pin0, dpin, dq, nsteps;  // v: pass-major item of argmin/scale/workspace, n: batch item
   {
     const int r = chain_id >> 1;
     if (!CROSS) {
       db = (chain_id & 1) ? UP : DOWN;
-      n = r / a.W;
+      v = r / a.W;
       const int x = r % a.W;
       nsteps = a.H - 1;
       pin0 = (db == DOWN) ? a.W + x : (a.H - 2) * a.W + x;  // DOWN: y = 1.., UP: y = H-2..
@@ -159,13 +164,14 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
       dq = -dpin;
     } else {
       db = (chain_id & 1) ? RIGHT : LEFT;
-      n = r / a.H;
+      v = r / a.H;
       const int y = r % a.H;
       nsteps = a.W - 1;
       pin0 = (db == LEFT) ? y * a.W + a.W - 2 : y * a.W + 1;  // LEFT: x = W-2.., RIGHT: x = 1..
       dpin = (db == LEFT) ? -1 : 1;
       dq = -dpin;
     }
+    n = v % a.B;
   }
   const int fd = db ^ 1;
   const bool stereo = (VARIANT == BPL_LBP_STEREO);
@@ -174,12 +180,12 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
   const uint32_t am_size = (a.argmin_kind == BPL_ARGMIN_U8) ? 1u : (a.argmin_kind == BPL_ARGMIN_U16 ? 2u : 4u);
   const T* msgs_db = static_cast<const T*>(a.msgs) + (static_cast<int64_t>(n) * 4 + db) * HWL;
   const T* grad_db = static_cast<const T*>(a.in_grad) + (static_cast<int64_t>(n) * 4 + db) * HWL;
-  const uint8_t* am_db = static_cast<const uint8_t*>(a.argmin) + (static_cast<int64_t>(n) * 4 + db) * HWL * am_size;
-  const float* saved_up = a.saved + (static_cast<int64_t>(n) * 2 + 0) * HWL;
-  const float* saved_dn = a.saved + (static_cast<int64_t>(n) * 2 + 1) * HWL;
-  float* saved_out = a.saved + (static_cast<int64_t>(n) * 2 + (db == UP ? 0 : 1)) * HWL;
+  const uint8_t* am_db = static_cast<const uint8_t*>(a.argmin) + (static_cast<int64_t>(v) * 4 + db) * HWL * am_size;
+  const float* saved_up = a.saved + (static_cast<int64_t>(v) * 2 + 0) * HWL;
+  const float* saved_dn = a.saved + (static_cast<int64_t>(v) * 2 + 1) * HWL;
+  float* saved_out = a.saved + (static_cast<int64_t>(v) * 2 + (db == UP ? 0 : 1)) * HWL;
   float* gcost_n = a.grad_cost + static_cast<int64_t>(n) * HWL;
-  const float* scale_db = a.scale + (static_cast<int64_t>(n) * 4 + db) * HW;
+  const float* scale_db = a.scale + (static_cast<int64_t>(v) * 4 + db) * HW;
   const float* edge_fd = a.edge + (static_cast<int64_t>(ne) * 4 + fd) * HW;
   const float* jump_fd = stereo ? a.jump + (static_cast<int64_t>(nj) * 4 + fd) * a.Lv * HW : nullptr;
   float* gjump_fd = stereo ? a.grad_jump + (static_cast<int64_t>(nj) * 4 + fd) * a.Lv * HW : nullptr;
@@ -513,7 +519,7 @@ int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
                    "cudaFuncSetAttribute");
     }
     a.phase = phase;
-    a.nchains = 2 * a.B * (phase == 0 ? a.W : a.H);
+    a.nchains = 2 * a.B * a.reps * (phase == 0 ? a.W : a.H);
     const int blocks = (a.nchains + wpb - 1) / wpb;
     kern<<<blocks, 32 * wpb, smem, stream>>>(a);
     BPL_CUDA_TRY(cudaGetLastError(), "lbp_backward launch");

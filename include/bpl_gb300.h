@@ -142,6 +142,33 @@ int bpl_lbp_backward(int variant, const float* jump, const float* edge, const fl
                      int edge_batch, void* stream);
 
 /*
+ * Reference adjoint of `passes` LBP passes run in place on one messages
+ * tensor (the reference's iteration loop, message_passing_op_cuda.py:161-168):
+ * its backward of every pass reads the same messages (the last pass's, the
+ * tensor having been overwritten) and the same in_grad (the message gradient
+ * it returns is in_grad), so the passes' adjoints are independent and run
+ * here as one launch.  argmin (passes,B,4,H,W,L) and scale (passes,B,4,H,W)
+ * are stacked in pass order; grad_cost, grad_jump and grad_edge receive the
+ * sum over the passes (what the reference's autograd accumulates).
+ * workspace: passes * bpl_lbp_backward_workspace_size(B, H, W, L) bytes.
+ * No counterpart in the reference (one call per pass there); other
+ * arguments as bpl_lbp_backward.
+ */
+int bpl_lbp_backward_passes(int variant, const float* jump, const float* edge, const float* in_grad,
+                            const float* messages, const void* argmin, int argmin_kind, const float* scale,
+                            float* grad_cost, float* grad_jump, float* grad_edge, void* workspace,
+                            size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
+                            int edge_batch, int passes, void* stream);
+
+/* The same for FP16 storage (layout of bpl_lbp_backward_f16; workspace
+ * passes * bpl_lbp_backward_workspace_size(B, H, W, Lp) bytes). */
+int bpl_lbp_backward_passes_f16(int variant, const float* jump, const float* edge, const void* in_grad,
+                                const void* messages, const void* argmin, int argmin_kind, const float* scale,
+                                float* grad_cost, float* grad_jump, float* grad_edge, void* workspace,
+                                size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
+                                int edge_batch, int passes, void* stream);
+
+/*
  * Exact adjoint of one LBP pass (FP32 storage).  No counterpart in the
  * reference, whose adjoint (bpl_lbp_backward) returns in_grad as the message
  * gradient; the cost, jump and edge gradients are the reference adjoint's

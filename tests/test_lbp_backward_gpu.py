@@ -121,3 +121,41 @@ def test_backward_full_size():
     gin = g.normal(0, 1, size=(B, 4, H, W, L)).astype(np.float32)
     fwd, bwd = run_case(0, cost, jump, edge, msgs, 3, gin, argmin_dtype=torch.uint8)
     check(0, fwd, bwd, jump, edge, gin, "c1")
+
+
+@pytest.mark.parametrize("half", [False, True], ids=["fp32", "fp16"])
+def test_backward_passes_equals_sum_of_single_passes(half):
+    """bpl_lbp_backward_passes (the passes' reference adjoints in one launch)
+    equals the sum of one bpl_lbp_backward per pass."""
+    from bpl_gb300 import ops
+    dev = torch.device("cuda:0")
+    g = cases.rng(17)
+    B, H, W, L, P = 2, 13, 21, 40, 3
+    cost = torch.from_numpy(cases.random_cost(g, B, H, W, L)).to(dev)
+    edge = torch.from_numpy(cases.edge_weights(g, B, H, W)).to(dev)
+    jump = torch.from_numpy(cases.stereo_taps(1, H, W, 0.1, 0.5)).to(dev)
+    Ls = ops.padded_labels(L) if half else L
+    gin = torch.randn((B, 4, H, W, L), device=dev, generator=torch.Generator(device=dev).manual_seed(3))
+    if half:
+        ch = ops.to_half_padded(cost, L)
+        m = torch.zeros((B, 4, H, W, Ls), dtype=torch.float16, device=dev)
+        gin = ops.to_half_padded(gin, L)
+    else:
+        m = torch.zeros((B, 4, H, W, L), device=dev)
+    ams = torch.empty((P, B, 4, H, W, Ls), dtype=torch.uint8, device=dev)
+    scs = torch.empty((P, B, 4, H, W), device=dev)
+    for k in range(P):
+        if half:
+            ops.lbp_forward_f16(0, ch, jump, edge, m, 3, L, argmin=ams[k], scale=scs[k])
+        else:
+            ops.lbp_forward(0, cost, jump, edge, m, 3, argmin_dtype=torch.uint8, argmin=ams[k], scale=scs[k])
+    gc, gj, ge = ops.lbp_backward_passes(0, jump, edge, gin, m, ams, scs, L=L)
+    sc_, sj, se = 0, 0, 0
+    for k in range(P):
+        if half:
+            a, b, c = ops.lbp_backward_f16(0, jump, edge, gin, m, ams[k], scs[k], L)
+        else:
+            a, b, c, _ = ops.lbp_backward(0, jump, edge, gin, m, ams[k], scs[k])
+        sc_, sj, se = sc_ + a, sj + b, se + c
+    for got, want in ((gc, sc_), (gj, sj), (ge, se)):
+        assert (got - want).abs().max().item() <= 1e-4 * max(1.0, want.abs().max().item())
