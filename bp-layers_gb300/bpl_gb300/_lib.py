@@ -27,8 +27,10 @@ SIGNATURES = {
     "bpl_lbp_backward": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 5 + [ctypes.c_size_t] + [c_int] * 7 + [c_void_p],
     "bpl_lbp_backward_f16": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 5 + [ctypes.c_size_t] + [c_int] * 7 + [c_void_p],
     "bpl_lbp_backward_exact": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 6 + [ctypes.c_size_t] + [c_int] * 7 + [c_void_p],
-    "bpl_lbp_backward_passes": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 5 + [ctypes.c_size_t] + [c_int] * 8 + [c_void_p],
-    "bpl_lbp_backward_passes_f16": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 5 + [ctypes.c_size_t] + [c_int] * 8 + [c_void_p],
+    "bpl_lbp_backward_passes": [c_int] + [c_void_p] * 3 + [ctypes.c_int64] * 2 + [c_void_p] * 2 + [c_int] + [c_void_p] * 5 + [ctypes.c_size_t] + [c_int] * 8 + [c_void_p],
+    "bpl_lbp_backward_passes_f16": [c_int] + [c_void_p] * 3 + [ctypes.c_int64] * 2 + [c_void_p] * 2 + [c_int] + [c_void_p] * 5 + [ctypes.c_size_t] + [c_int] * 8 + [c_void_p],
+    "bpl_beliefs_forward": [c_void_p, c_int] + [c_void_p] * 3 + [c_int] * 5 + [c_void_p],
+    "bpl_beliefs_backward": [c_void_p, c_int] + [c_void_p] * 6 + [c_int] * 5 + [c_void_p],
     "bpl_sad_volume_depth": [c_int, c_int, c_float],
     "bpl_sad_forward": [c_void_p] * 3 + [c_int] * 6 + [c_float, c_void_p],
     "bpl_sad_backward": [c_void_p] * 5 + [c_int] * 7 + [c_void_p],

@@ -11,7 +11,7 @@ import torch
 import torch.nn as nn
 
 from .. import ops
-from .stereo import Inference, TemperatureSoftmin  # noqa: F401  (Inference is shared)
+from .stereo import BeliefsSoftmin, Inference, TemperatureSoftmin  # noqa: F401  (Inference is shared)
 
 
 def _argmin_dtype(L):
@@ -86,8 +86,7 @@ class MessagePassingGlobal(nn.Module):
         for _ in range(self.max_iter):
             messages = LBPMinSumFunctionGlobal.apply(cost, self.L1, self.L2, edge_weights, messages, self.delta,
                                                      jump, torch.tensor(single_pw))
-        beliefs = messages.sum(dim=1) + cost
-        return self.softmin.forward(beliefs)
+        return BeliefsSoftmin.apply(messages, cost, self.softmin.T)
 
 
 class LBPMinSumFunctionPixel(torch.autograd.Function):
@@ -150,5 +149,4 @@ class MessagePassingPixel(nn.Module):
         cost = -prob_vol
         for _ in range(self.max_iter):
             messages = LBPMinSumFunctionPixel.apply(cost, self.L1, self.L2, edge_weights, messages, self.delta, jump)
-        beliefs = messages.sum(dim=1) + cost
-        return self.softmin.forward(beliefs)
+        return BeliefsSoftmin.apply(messages, cost, self.softmin.T)

@@ -31,6 +31,36 @@ class TemperatureSoftmin(nn.Module):
         return F.softmin(x / self.T, dim=self.dim)
 
 
+class BeliefsSoftmin(torch.autograd.Function):
+    """softmin((sum_k messages[:, k] + cost) / T) over the label axis, fused
+    (message_passing_op_cuda.py:170-173 with TemperatureSoftmin,
+    corenet.py:106-113): one kernel each way instead of the separate torch
+    passes.  forward(messages (B,4,H,W,Ls) float or half, cost (B,H,W,L),
+    T (1,)).  The gradient of z = sum + cost goes to the cost and, as a
+    stride-0 view, to every message slot (no copy)."""
+
+    @staticmethod
+    def forward(ctx, messages, cost, T):
+        cost = cost.contiguous()
+        beliefs = ops.beliefs_forward(messages, cost, T)
+        ctx.save_for_backward(messages, cost, T, beliefs)
+        return beliefs
+
+    @staticmethod
+    def backward(ctx, grad_beliefs):
+        messages, cost, T, beliefs = ctx.saved_tensors
+        gz, gT = ops.beliefs_backward(messages, cost, T, beliefs, grad_beliefs, want_temperature=ctx.needs_input_grad[2])
+        B, _, H, W, Ls = messages.shape
+        L = cost.shape[-1]
+        if messages.dtype == torch.float16:
+            g1 = torch.zeros((B, 1, H, W, Ls), dtype=torch.float16, device=gz.device)
+            g1[:, 0, ..., :L] = gz
+        else:
+            g1 = gz.unsqueeze(1)
+        gm = g1.expand(B, 4, H, W, Ls)
+        return gm, gz, (gT.view_as(T) if gT is not None else None)
+
+
 def pack_affinities(affinities, offset):
     """(N,4,K,H,W) affinities [L2-, L2+, L1-, L1+, L3] (or [L1, L1, L2]) plus
     offset (N,4,H,W) -> (N,4,K+3,H,W) jump taps [offset, L3, L2-, L1-, 0, L1+,
@@ -246,8 +276,7 @@ class MessagePassing(nn.Module):
                 messages = m.requires_grad_(True)
             messages = LBPMinSumLoop.apply(cost, cost_h, edge_weights, messages, self.delta, affinities, offset,
                                            self.max_iter)
-            beliefs = messages[..., :C].float().sum(dim=1) + cost
-            return self.softmin.forward(beliefs), messages
+            return BeliefsSoftmin.apply(messages, cost, self.softmin.T), messages
         if self.adjoint == "reference":
             messages = LBPMinSumLoop.apply(cost, None, edge_weights, messages, self.delta, affinities, offset,
                                            self.max_iter)
@@ -255,9 +284,7 @@ class MessagePassing(nn.Module):
             for _ in range(self.max_iter):
                 messages = LBPMinSumFunction.apply(cost, edge_weights, messages, self.delta, affinities, offset,
                                                    self.adjoint)
-        beliefs = messages.sum(dim=1) + cost
-        beliefs = self.softmin.forward(beliefs)
-        return beliefs, messages
+        return BeliefsSoftmin.apply(messages, cost, self.softmin.T), messages
 
 
 class Inference(nn.Module):

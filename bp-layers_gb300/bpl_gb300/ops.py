@@ -375,7 +375,15 @@ def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.T
     L given).  Returns (grad_cost, grad_jump, grad_edge) summed over the
     passes; the message gradient is in_grad."""
     half = messages.dtype == torch.float16
-    _check_input("in_grad", in_grad, dtype=messages.dtype, dim=5)
+    if not isinstance(in_grad, torch.Tensor) or in_grad.dtype != messages.dtype or in_grad.dim() != 5 \
+            or not in_grad.is_cuda:
+        raise BplError("in_grad must be a CUDA tensor of the messages' dtype and rank")
+    # a (B,4,H,W,Ls) gradient, contiguous or the beliefs' (B,1,H,W,Ls)
+    # gradient expanded over the four slots (slot stride 0): no copy
+    if in_grad.shape[1] != 4 or in_grad.stride(4) != 1 or in_grad.stride(3) != in_grad.shape[4] \
+            or in_grad.stride(2) != in_grad.shape[3] * in_grad.shape[4]:
+        in_grad = in_grad.contiguous()
+    g_bstride, g_sstride = in_grad.stride(0), in_grad.stride(1)
     _check_input("messages", messages, dtype=None, dim=5)
     _check_input("argmins", argmins, dtype=None, dim=6)
     _check_input("scales", scales, dim=5)
@@ -410,8 +418,43 @@ def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.T
     fn = lib().bpl_lbp_backward_passes_f16 if half else lib().bpl_lbp_backward_passes
     name = "lbp_backward_f16" if half else "lbp_backward"
     st = _timed(name, lambda: fn(
-        variant, _ptr(jump) if variant != LBP_SEM_PIXEL else None, _ptr(edge), _ptr(in_grad), _ptr(messages),
-        _ptr(argmins), kind, _ptr(scales), _ptr(grad_cost), _ptr(grad_jump), _ptr(grad_edge), _ptr(workspace),
+        variant, _ptr(jump) if variant != LBP_SEM_PIXEL else None, _ptr(edge), _ptr(in_grad), g_bstride, g_sstride,
+        _ptr(messages), _ptr(argmins), kind, _ptr(scales), _ptr(grad_cost), _ptr(grad_jump), _ptr(grad_edge), _ptr(workspace),
         workspace.numel() * workspace.element_size(), B, H, W, L, Lv, jb, edge.shape[0], P, _stream(messages)))
     check(st, "bpl_lbp_backward_passes")
     return grad_cost, grad_jump, grad_edge
+
+
+def beliefs_forward(messages: torch.Tensor, cost: torch.Tensor, temperature: torch.Tensor, L: int | None = None,
+                    out: torch.Tensor | None = None) -> torch.Tensor:
+    """softmin(((((M0+M1)+M2)+M3)+cost)/T) over labels, fused (one pass).
+    messages (B,4,H,W,Ls) float or half (padded), cost (B,H,W,L) float,
+    temperature a one-element float CUDA tensor."""
+    _check_input("messages", messages, dtype=None, dim=5)
+    _check_input("cost", cost, dim=4)
+    B, _, H, W, Ls = messages.shape
+    L = cost.shape[-1] if L is None else L
+    if out is None:
+        out = torch.empty((B, H, W, L), dtype=torch.float32, device=cost.device)
+    st = _timed("beliefs_forward", lambda: lib().bpl_beliefs_forward(
+        _ptr(messages), int(messages.dtype == torch.float16), _ptr(cost), _ptr(temperature), _ptr(out),
+        B, H, W, L, Ls, _stream(cost)))
+    check(st, "bpl_beliefs_forward")
+    return out
+
+
+def beliefs_backward(messages: torch.Tensor, cost: torch.Tensor, temperature: torch.Tensor, beliefs: torch.Tensor,
+                     grad_beliefs: torch.Tensor, want_temperature: bool = True):
+    """Gradient of the fused epilogue: (grad_z (B,H,W,L), grad_T (1,) or None)."""
+    _check_input("beliefs", beliefs, dim=4)
+    grad_beliefs = grad_beliefs.contiguous()
+    _check_input("grad_beliefs", grad_beliefs, dim=4)
+    B, _, H, W, Ls = messages.shape
+    L = beliefs.shape[-1]
+    gz = torch.empty_like(beliefs)
+    gT = torch.empty(1, dtype=torch.float32, device=beliefs.device) if want_temperature else None
+    st = _timed("beliefs_backward", lambda: lib().bpl_beliefs_backward(
+        _ptr(messages), int(messages.dtype == torch.float16), _ptr(cost), _ptr(temperature), _ptr(beliefs),
+        _ptr(grad_beliefs), _ptr(gz), _ptr(gT), B, H, W, L, Ls, _stream(beliefs)))
+    check(st, "bpl_beliefs_backward")
+    return gz, gT

@@ -1,0 +1,207 @@
+// Fused belief epilogue of the BP layer:
+//   beliefs = softmin(((((M0 + M1) + M2) + M3) + cost) / T)   over labels
+// (the reference computes messages.sum(dim=1) + cost and then
+// TemperatureSoftmin as separate torch passes:
+// ops/lbp_stereo/message_passing_op_cuda.py:170-173, corenet.py:106-113),
+// and its backward: the gradient of z = sum + cost (which is also every
+// message slot's gradient) and of the temperature.
+//
+// One warp per pixel, labels lane + 32k, grid-stride over pixels.  HBM-bound
+// streaming: the forward reads the 4 message slots and the cost once and
+// writes the beliefs; the backward recomputes z from the same inputs, reads
+// the beliefs and their gradient and writes the gradient of z.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "bpl_device.cuh"
+#include "bpl_internal.h"
+
+namespace bpl {
+namespace {
+
+template <typename T>
+__device__ __forceinline__ float tof(T v);
+template <>
+__device__ __forceinline__ float tof<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float tof<__half>(__half v) { return __half2float(v); }
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL, v, o));
+  return v;
+}
+
+// z / T for the labels of one pixel (K per lane); invalid labels -> +inf.
+template <int K, typename T>
+__device__ __forceinline__ void load_z(const T* msgs, const float* cost, int64_t pix, int64_t HWLs, int Ls, int L,
+                                       int n, int64_t HW, float Tm, int lane, float (&zt)[K]) {
+  const int64_t p = pix % HW;
+  const T* m = msgs + (static_cast<int64_t>(n) * 4) * HWLs + p * Ls;
+  const float* c = cost + pix * L;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int t = lane + 32 * k;
+    if (t < L) {
+      const float s = __fadd_rn(__fadd_rn(__fadd_rn(tof<T>(m[t]), tof<T>(m[HWLs + t])), tof<T>(m[2 * HWLs + t])),
+                                tof<T>(m[3 * HWLs + t]));
+      zt[k] = __fdiv_rn(__fadd_rn(s, c[t]), Tm);
+    } else {
+      zt[k] = __int_as_float(0x7f800000);
+    }
+  }
+}
+
+template <int K, typename T>
+__global__ void __launch_bounds__(256) beliefs_fwd_kernel(const T* msgs, const float* cost, const float* Tp, float* out,
+                                                          int B, int H, int W, int L, int Ls) {
+  const int lane = threadIdx.x & 31;
+  const int64_t HW = static_cast<int64_t>(H) * W;
+  const int64_t npix = B * HW;
+  const int64_t HWLs = HW * Ls;
+  const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  const float Tm = __ldg(Tp);
+  for (int64_t pix = blockIdx.x * static_cast<int64_t>(blockDim.x >> 5) + (threadIdx.x >> 5); pix < npix;
+       pix += warps) {
+    const int n = static_cast<int>(pix / HW);
+    float zt[K];
+    load_z<K, T>(msgs, cost, pix, HWLs, Ls, L, n, HW, Tm, lane, zt);
+    // softmin(x) = softmax(-x): shift by the minimum of x
+    float mn = zt[0];
+#pragma unroll
+    for (int k = 1; k < K; ++k) mn = fminf(mn, zt[k]);
+    mn = -warp_max(-mn);
+    float e[K], s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      e[k] = (lane + 32 * k < L) ? expf(mn - zt[k]) : 0.0f;
+      s += e[k];
+    }
+    s = warp_sum(s);
+    const float inv = 1.0f / s;
+    float* o = out + pix * L;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (lane + 32 * k < L) o[lane + 32 * k] = e[k] * inv;
+  }
+}
+
+template <int K, typename T>
+__global__ void __launch_bounds__(256) beliefs_bwd_kernel(const T* msgs, const float* cost, const float* Tp,
+                                                          const float* y, const float* gy, float* gz, float* gT,
+                                                          int B, int H, int W, int L, int Ls) {
+  const int lane = threadIdx.x & 31;
+  const int64_t HW = static_cast<int64_t>(H) * W;
+  const int64_t npix = B * HW;
+  const int64_t HWLs = HW * Ls;
+  const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  const float Tm = __ldg(Tp);
+  float tacc = 0.0f;
+  for (int64_t pix = blockIdx.x * static_cast<int64_t>(blockDim.x >> 5) + (threadIdx.x >> 5); pix < npix;
+       pix += warps) {
+    const int n = static_cast<int>(pix / HW);
+    float zt[K];
+    if (gT != nullptr) load_z<K, T>(msgs, cost, pix, HWLs, Ls, L, n, HW, Tm, lane, zt);
+    const float* yp = y + pix * L;
+    const float* gp = gy + pix * L;
+    float yv[K], gv[K], d = 0.0f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int t = lane + 32 * k;
+      yv[k] = (t < L) ? yp[t] : 0.0f;
+      gv[k] = (t < L) ? gp[t] : 0.0f;
+      d += yv[k] * gv[k];
+    }
+    d = warp_sum(d);
+    float* o = gz + pix * L;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int t = lane + 32 * k;
+      // u = -z/T: du = y (g - sum(y g)); dz = -du / T; dT += du * z / T^2
+      const float du = yv[k] * (gv[k] - d);
+      if (t < L) {
+        o[t] = -du / Tm;
+        if (gT != nullptr) tacc += du * (zt[k] / Tm);
+      }
+    }
+  }
+  if (gT != nullptr) {
+    tacc = warp_sum(tacc);
+    if (lane == 0 && tacc != 0.0f) atomicAdd(gT, tacc);
+  }
+}
+
+int grid_for(int64_t npix) {
+  const int64_t blocks = (npix + 7) / 8;  // 8 warps per block
+  return static_cast<int>(std::min<int64_t>(blocks, static_cast<int64_t>(sm_count()) * 16));
+}
+
+template <typename T>
+int fwd_impl(const T* msgs, const float* cost, const float* Tm, float* out, int B, int H, int W, int L, int Ls,
+             cudaStream_t s) {
+  const int g = grid_for(static_cast<int64_t>(B) * H * W);
+  const int k = (L + 31) / 32;
+#define BPL_BFWD(KK) beliefs_fwd_kernel<KK, T><<<g, 256, 0, s>>>(msgs, cost, Tm, out, B, H, W, L, Ls)
+  if (k <= 1) BPL_BFWD(1);
+  else if (k <= 2) BPL_BFWD(2);
+  else if (k <= 4) BPL_BFWD(4);
+  else if (k <= 6) BPL_BFWD(6);
+  else if (k <= 8) BPL_BFWD(8);
+  else if (k <= 16) BPL_BFWD(16);
+  else BPL_BFWD(32);
+#undef BPL_BFWD
+  BPL_CUDA_TRY(cudaGetLastError(), "beliefs_forward launch");
+  return BPL_OK;
+}
+
+template <typename T>
+int bwd_impl(const T* msgs, const float* cost, const float* Tm, const float* y, const float* gy, float* gz, float* gT,
+             int B, int H, int W, int L, int Ls, cudaStream_t s) {
+  if (gT) BPL_CUDA_TRY(cudaMemsetAsync(gT, 0, sizeof(float), s), "beliefs_backward: memset");
+  const int g = grid_for(static_cast<int64_t>(B) * H * W);
+  const int k = (L + 31) / 32;
+#define BPL_BBWD(KK) beliefs_bwd_kernel<KK, T><<<g, 256, 0, s>>>(msgs, cost, Tm, y, gy, gz, gT, B, H, W, L, Ls)
+  if (k <= 1) BPL_BBWD(1);
+  else if (k <= 2) BPL_BBWD(2);
+  else if (k <= 4) BPL_BBWD(4);
+  else if (k <= 6) BPL_BBWD(6);
+  else if (k <= 8) BPL_BBWD(8);
+  else if (k <= 16) BPL_BBWD(16);
+  else BPL_BBWD(32);
+#undef BPL_BBWD
+  BPL_CUDA_TRY(cudaGetLastError(), "beliefs_backward launch");
+  return BPL_OK;
+}
+
+}  // namespace
+}  // namespace bpl
+
+using namespace bpl;
+
+extern "C" int bpl_beliefs_forward(const void* messages, int messages_half, const float* cost,
+                                   const float* temperature, float* beliefs, int B, int H, int W, int L, int Ls,
+                                   void* stream) {
+  BPL_REQUIRE(messages && cost && beliefs && temperature, "beliefs_forward: null pointer");
+  BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1 && L >= 1 && L <= 1024 && Ls >= L, "beliefs_forward: bad shape");
+  if (messages_half)
+    return fwd_impl(static_cast<const __half*>(messages), cost, temperature, beliefs, B, H, W, L, Ls,
+                    as_stream(stream));
+  return fwd_impl(static_cast<const float*>(messages), cost, temperature, beliefs, B, H, W, L, Ls,
+                  as_stream(stream));
+}
+
+extern "C" int bpl_beliefs_backward(const void* messages, int messages_half, const float* cost,
+                                    const float* temperature, const float* beliefs, const float* grad_beliefs,
+                                    float* grad_z, float* grad_temperature, int B, int H, int W, int L, int Ls,
+                                    void* stream) {
+  BPL_REQUIRE(beliefs && grad_beliefs && grad_z && temperature, "beliefs_backward: null pointer");
+  BPL_REQUIRE(grad_temperature == nullptr || (messages && cost), "beliefs_backward: null messages/cost");
+  BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1 && L >= 1 && L <= 1024 && Ls >= L, "beliefs_backward: bad shape");
+  if (messages_half)
+    return bwd_impl(static_cast<const __half*>(messages), cost, temperature, beliefs, grad_beliefs, grad_z,
+                    grad_temperature, B, H, W, L, Ls, as_stream(stream));
+  return bwd_impl(static_cast<const float*>(messages), cost, temperature, beliefs, grad_beliefs, grad_z,
+                  grad_temperature, B, H, W, L, Ls, as_stream(stream));
+}

@@ -56,7 +56,8 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
                       const void* messages, const void* argmin, int argmin_kind, const float* scale,
                       float* grad_cost, float* grad_jump, float* grad_edge, void* workspace, size_t workspace_bytes,
                       int B, int H, int W, int L, int Lv, int jump_batch, int edge_batch, void* stream,
-                      float* grad_messages = nullptr, int reps = 1) {
+                      float* grad_messages = nullptr, int reps = 1, int64_t g_bstride = -1,
+                      int64_t g_sstride = -1) {
   BPL_REQUIRE(variant >= 0 && variant <= 2, "lbp_backward: unknown variant %d", variant);
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1, "lbp_backward: bad shape B=%d H=%d W=%d", B, H, W);
   BPL_REQUIRE(H <= 65535 && W <= 65535, "lbp_backward: H and W must be <= 65535");
@@ -104,6 +105,8 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   a.saved = static_cast<float*>(workspace);
   a.gmsg = grad_messages;
   a.reps = reps;
+  a.g_bstride = (g_bstride < 0) ? 4 * HW * Ls : g_bstride;
+  a.g_sstride = (g_sstride < 0) ? HW * Ls : g_sstride;
   a.B = B;
   a.H = H;
   a.W = W;
@@ -164,24 +167,28 @@ extern "C" int bpl_lbp_backward_exact(int variant, const float* jump, const floa
 }
 
 extern "C" int bpl_lbp_backward_passes(int variant, const float* jump, const float* edge, const float* in_grad,
+                                       int64_t in_grad_batch_stride, int64_t in_grad_slot_stride,
                                        const float* messages, const void* argmin, int argmin_kind,
                                        const float* scale, float* grad_cost, float* grad_jump, float* grad_edge,
                                        void* workspace, size_t workspace_bytes, int B, int H, int W, int L, int Lv,
                                        int jump_batch, int edge_batch, int passes, void* stream) {
+  BPL_REQUIRE(in_grad_batch_stride >= 0 && in_grad_slot_stride >= 0, "lbp_backward_passes: negative stride");
   return lbp_backward_impl(0, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
-                           stream, nullptr, passes);
+                           stream, nullptr, passes, in_grad_batch_stride, in_grad_slot_stride);
 }
 
 extern "C" int bpl_lbp_backward_passes_f16(int variant, const float* jump, const float* edge, const void* in_grad,
+                                           int64_t in_grad_batch_stride, int64_t in_grad_slot_stride,
                                            const void* messages, const void* argmin, int argmin_kind,
                                            const float* scale, float* grad_cost, float* grad_jump,
                                            float* grad_edge, void* workspace, size_t workspace_bytes, int B, int H,
                                            int W, int L, int Lv, int jump_batch, int edge_batch, int passes,
                                            void* stream) {
+  BPL_REQUIRE(in_grad_batch_stride >= 0 && in_grad_slot_stride >= 0, "lbp_backward_passes: negative stride");
   return lbp_backward_impl(1, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
-                           stream, nullptr, passes);
+                           stream, nullptr, passes, in_grad_batch_stride, in_grad_slot_stride);
 }
 
 extern "C" int bpl_lbp_backward_f16(int variant, const float* jump, const float* edge, const void* in_grad,

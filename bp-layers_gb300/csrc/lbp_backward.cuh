@@ -61,6 +61,11 @@ struct BwdArgs {
   // (reps, B, ...); the chains of all passes run in one launch and their
   // gradients accumulate into the same outputs
   int reps;
+  // in_grad strides (elements) between batch items and between message
+  // slots: 4*H*W*Ls and H*W*Ls for a (B,4,H,W,Ls) tensor; a slot stride of
+  // 0 reads one (B,H,W,Ls) gradient for every slot (the beliefs' gradient
+  // broadcast over the four messages)
+  int64_t g_bstride, g_sstride;
   int Ls;
   int argmin_kind;
   int phase;  // 0: DOWN+UP over columns, 1: LEFT+RIGHT over rows
@@ -179,7 +184,7 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
   const int ne = (a.eb == 1) ? 0 : n;
   const uint32_t am_size = (a.argmin_kind == BPL_ARGMIN_U8) ? 1u : (a.argmin_kind == BPL_ARGMIN_U16 ? 2u : 4u);
   const T* msgs_db = static_cast<const T*>(a.msgs) + (static_cast<int64_t>(n) * 4 + db) * HWL;
-  const T* grad_db = static_cast<const T*>(a.in_grad) + (static_cast<int64_t>(n) * 4 + db) * HWL;
+  const T* grad_db = static_cast<const T*>(a.in_grad) + n * a.g_bstride + db * a.g_sstride;
   const uint8_t* am_db = static_cast<const uint8_t*>(a.argmin) + (static_cast<int64_t>(v) * 4 + db) * HWL * am_size;
   const float* saved_up = a.saved + (static_cast<int64_t>(v) * 2 + 0) * HWL;
   const float* saved_dn = a.saved + (static_cast<int64_t>(v) * 2 + 1) * HWL;

@@ -25,6 +25,7 @@
 #define BPL_GB300_H
 
 #include <stddef.h>
+#include <stdint.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -150,11 +151,16 @@ int bpl_lbp_backward(int variant, const float* jump, const float* edge, const fl
  * here as one launch.  argmin (passes,B,4,H,W,L) and scale (passes,B,4,H,W)
  * are stacked in pass order; grad_cost, grad_jump and grad_edge receive the
  * sum over the passes (what the reference's autograd accumulates).
+ * in_grad is read with the given strides in elements between batch items
+ * and between message slots (4*H*W*L and H*W*L for a (B,4,H,W,L) tensor;
+ * slot stride 0 reads one (B,H,W,L) gradient for all four slots, which is
+ * what the beliefs' sum over the slots produces).
  * workspace: passes * bpl_lbp_backward_workspace_size(B, H, W, L) bytes.
  * No counterpart in the reference (one call per pass there); other
  * arguments as bpl_lbp_backward.
  */
 int bpl_lbp_backward_passes(int variant, const float* jump, const float* edge, const float* in_grad,
+                            int64_t in_grad_batch_stride, int64_t in_grad_slot_stride,
                             const float* messages, const void* argmin, int argmin_kind, const float* scale,
                             float* grad_cost, float* grad_jump, float* grad_edge, void* workspace,
                             size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
@@ -163,6 +169,7 @@ int bpl_lbp_backward_passes(int variant, const float* jump, const float* edge, c
 /* The same for FP16 storage (layout of bpl_lbp_backward_f16; workspace
  * passes * bpl_lbp_backward_workspace_size(B, H, W, Lp) bytes). */
 int bpl_lbp_backward_passes_f16(int variant, const float* jump, const float* edge, const void* in_grad,
+                                int64_t in_grad_batch_stride, int64_t in_grad_slot_stride,
                                 const void* messages, const void* argmin, int argmin_kind, const float* scale,
                                 float* grad_cost, float* grad_jump, float* grad_edge, void* workspace,
                                 size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
@@ -189,6 +196,28 @@ int bpl_lbp_backward_exact(int variant, const float* jump, const float* edge, co
                            float* grad_cost, float* grad_jump, float* grad_edge, float* grad_messages,
                            void* workspace, size_t workspace_bytes, int B, int H, int W, int L, int Lv,
                            int jump_batch, int edge_batch, void* stream);
+
+/*
+ * Fused belief epilogue (no counterpart in the reference, which runs
+ * messages.sum(dim=1) + cost and TemperatureSoftmin as separate torch
+ * passes: ops/lbp_stereo/message_passing_op_cuda.py:170-173,
+ * corenet.py:106-113).  beliefs (B,H,W,L) = softmin(z / T) over labels with
+ * z = (((M0 + M1) + M2) + M3) + cost; messages (B,4,H,W,Ls) float
+ * (messages_half = 0) or half (1, Ls = L rounded up to 8), cost (B,H,W,L);
+ * temperature: one device float (read on the device, so no host sync).
+ */
+int bpl_beliefs_forward(const void* messages, int messages_half, const float* cost, const float* temperature,
+                        float* beliefs, int B, int H, int W, int L, int Ls, void* stream);
+
+/*
+ * Its backward: grad_z (B,H,W,L) = d loss / d z (also each message slot's
+ * gradient) from beliefs and grad_beliefs; grad_temperature (one device
+ * float, zeroed by this call, may be NULL) = d loss / d T, for which z is
+ * recomputed from messages and cost.
+ */
+int bpl_beliefs_backward(const void* messages, int messages_half, const float* cost, const float* temperature,
+                         const float* beliefs, const float* grad_beliefs, float* grad_z, float* grad_temperature,
+                         int B, int H, int W, int L, int Ls, void* stream);
 
 /* Disparity count D of the SAD volume: (int)((max_disp - min_disp + 1) / step)
  * (ops/sad/src/stereo_sad_kernel.cu:122); -1 for a non-positive step. */

@@ -120,3 +120,36 @@ def test_semantic_message_passing(kind):
     beliefs.sum().backward()
     assert p.grad is not None and torch.isfinite(p.grad).all()
     assert jin.grad is not None and jin.grad.shape == jin.shape and torch.isfinite(jin.grad).all()
+
+
+@pytest.mark.parametrize("half", [False, True], ids=["fp32", "fp16"])
+def test_fused_belief_epilogue_matches_torch(half):
+    """BeliefsSoftmin (one kernel each way) against torch's
+    softmin((messages.sum(1) + cost) / T): values and the gradients of the
+    messages, the cost and the temperature."""
+    from bpl_gb300 import ops
+    from bpl_gb300.layers.stereo import BeliefsSoftmin
+    dev = torch.device("cuda:0")
+    g = torch.Generator(device=dev).manual_seed(7)
+    B, H, W, L = 2, 9, 13, 70
+    Ls = ops.padded_labels(L) if half else L
+    m = torch.randn((B, 4, H, W, Ls), device=dev, generator=g)
+    if half:
+        m = m.half()
+    cost = torch.randn((B, H, W, L), device=dev, generator=g)
+    T = torch.tensor([0.7], device=dev)
+    up = torch.randn((B, H, W, L), device=dev, generator=g)
+
+    m1, c1, T1 = m.clone().requires_grad_(True), cost.clone().requires_grad_(True), T.clone().requires_grad_(True)
+    y1 = BeliefsSoftmin.apply(m1, c1, T1)
+    y1.backward(up)
+    m2, c2, T2 = m.clone().requires_grad_(True), cost.clone().requires_grad_(True), T.clone().requires_grad_(True)
+    z = (((m2[:, 0, ..., :L].float() + m2[:, 1, ..., :L].float()) + m2[:, 2, ..., :L].float())
+         + m2[:, 3, ..., :L].float()) + c2
+    y2 = torch.nn.functional.softmin(z / T2, dim=3)
+    y2.backward(up)
+    assert (y1 - y2).abs().max().item() <= 2e-6
+    assert (c1.grad - c2.grad).abs().max().item() <= 1e-5 * max(1.0, c2.grad.abs().max().item())
+    gm1, gm2 = m1.grad.float(), m2.grad.float()
+    assert (gm1 - gm2).abs().max().item() <= 2e-3 * max(1.0, gm2.abs().max().item())
+    assert abs(T1.grad.item() - T2.grad.item()) <= 1e-4 * max(1.0, abs(T2.grad.item()))
