@@ -257,8 +257,10 @@ __device__ __forceinline__ void load_taps(const FwdArgs& a, const Chain<T>& c, i
 //   code 1..4: R = code - 2 (R = -1: no offset beats the candidate)
 //   bit 8: the window holds tie-only offsets; the tile row Lv+1 then holds
 //          the tie-only tap of smallest product with w
+//   bit 9: every tie-only tap is bitwise L2
 constexpr int kWinGeneric = 0;
 constexpr int kWinHasTieOnly = 0x100;
+constexpr int kWinTieIsL2 = 0x200;  // every tie-only tap equals L2 bitwise
 
 __device__ __forceinline__ void store_taps(const FwdArgs& a, float* tile, int lane, const TapRegs& r,
                                            bool stereo) {
@@ -276,7 +278,7 @@ __device__ __forceinline__ void store_taps(const FwdArgs& a, float* tile, int la
     float fnr = 0.0f;
     if (tile[lane] == 0.0f && a.delta <= kFastDelta) {
       int R = -1;
-      bool ok = true, seen_tie = false, have_tie = false;
+      bool ok = true, seen_tie = false, have_tie = false, tie_l2 = true;
       for (int q = 0; q <= a.delta; ++q) {
         const float fp = tile[max(1, min(a.Lv - 1, a.Lv / 2 - q)) * 33 + lane];  // jd = +q
         const float fm = tile[max(1, min(a.Lv - 1, a.Lv / 2 + q)) * 33 + lane];  // jd = -q
@@ -287,6 +289,7 @@ __device__ __forceinline__ void store_taps(const FwdArgs& a, float* tile, int la
           R = q;
         } else if (tp && tm) {
           seen_tie = true;
+          tie_l2 = tie_l2 && __float_as_int(fp) == __float_as_int(L2) && __float_as_int(fm) == __float_as_int(L2);
           // tie-only tap of smallest product f*w
           const float f = (w >= 0.0f) ? fminf(fp, fm) : fmaxf(fp, fm);
           fnr = !have_tie ? f : ((w >= 0.0f) ? fminf(fnr, f) : fmaxf(fnr, f));
@@ -295,7 +298,7 @@ __device__ __forceinline__ void store_taps(const FwdArgs& a, float* tile, int la
           ok = false;
         }
       }
-      if (ok && R <= 2) code = (R + 2) | (have_tie ? kWinHasTieOnly : 0);
+      if (ok && R <= 2) code = (R + 2) | (have_tie ? kWinHasTieOnly : 0) | ((have_tie && tie_l2) ? kWinTieIsL2 : 0);
     }
     tile[(a.Lv + 1) * 33 + lane] = fnr;
     tile[(a.Lv + 2) * 33 + lane] = __int_as_float(code);
@@ -327,11 +330,16 @@ __device__ __forceinline__ void chain_sync(int id) {
 
 // K labels per lane over the chain (label = lane + 32k), KW = K/NW of them
 // owned by each of the chain's NW warps (slots [w*KW, (w+1)*KW)).
-// OCC: blocks per SM the register allocation must allow (1 for the
-// latency-bound phase with few scanlines, more where scanlines outnumber
-// the warps one wave holds).
+// OCC: blocks per SM the register allocation must allow.  1: 4-warp blocks
+// with every register the compiler wants (the latency-bound phase with few
+// scanlines); kHiOcc: 1-warp blocks, kHiOcc of them per SM (the phase whose
+// scanlines outnumber what a wave of 4-warp blocks holds).
+constexpr int kHiOcc = 17;
+template <int OCC>
+constexpr int fwd_block_warps() { return (OCC > 1) ? 1 : 4; }
+
 template <int K, int VARIANT, int NW, typename T, int OCC>
-__global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
+__global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_kernel(FwdArgs a) {
   constexpr bool kExact = sizeof(T) == 4;  // float storage: the reference's exact arithmetic
   static_assert(K % NW == 0, "labels must split evenly over the chain's warps");
   static_assert(NW == 1 || VARIANT != BPL_LBP_SEM_PIXEL, "pixel variant runs one warp per chain");
@@ -413,6 +421,10 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
                 ? static_cast<const T*>(a.jump) + static_cast<int64_t>(c.dir) * HW * L * a.Lm
                 : nullptr;
   c.t0 = 32 * KW * wic;
+  // label validity: with K = ceil(L/32) (the K <= 8 instantiations are
+  // dispatched exactly) only the last slot of a one-warp scanline can hold
+  // labels >= L; the test folds away for the other slots
+  auto lvalid = [&](int kk) -> bool { return (K <= 8 && NW == 1 && kk < KW - 1) || (c.t0 + lane + 32 * kk < L); };
   // labels copied per row: the warp's labels below Ls (padding included, so
   // half rows stay 16-byte sized)
   c.cnt = max(0, min(lroww, Ls - c.t0));
@@ -433,7 +445,7 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
 #pragma unroll
     for (int kk = 0; kk < KW; ++kk) {
       const int t = c.t0 + lane + 32 * kk;
-      const int64_t o = po + ((t < L) ? t : 0);  // labels >= L read label 0 (ignored)
+      const int64_t o = po + (lvalid(kk) ? t : 0);  // labels >= L read label 0 (ignored)
       ncst[kk] = __ldg(c.cost + o);
       nva[kk] = __ldg(c.slot_a + o);
       nvb[kk] = __ldg(c.slot_b + o);
@@ -459,7 +471,7 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
 #pragma unroll
     for (int kk = 0; kk < KW; ++kk) {
       const int t = c.t0 + lane + 32 * kk;
-      chain[kk] = (t < L) ? ldf<T>(src[t]) : 0.0f;
+      chain[kk] = lvalid(kk) ? ldf<T>(src[t]) : 0.0f;
     }
   }
 
@@ -509,7 +521,7 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
       const float vb = ldf<T>(kRing ? stg[2 * lroww + tl] : nvb[kk]);
       const float hv = (a.phase == 0) ? __fadd_rn(__fadd_rn(__fadd_rn(cst, chain[kk]), va), vb)
                                       : __fadd_rn(__fadd_rn(__fadd_rn(cst, va), vb), chain[kk]);
-      h[kk] = (c.t0 + tl < L) ? hv : kInf;
+      h[kk] = lvalid(kk) ? hv : kInf;
       cs.hs[c.t0 + tl] = h[kk];
     }
     // partial minimum over the warp's labels (one redux), with its tie count
@@ -666,8 +678,9 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
       // fast form, every window term is scanned.
       int R = -2;
       int s1 = -1;
+      int wcode = kWinGeneric;
       if (NW == 1 && stereo) {
-        const int wcode = __float_as_int(tile[(a.Lv + 2) * 33 + j]);
+        wcode = __float_as_int(tile[(a.Lv + 2) * 33 + j]);
         if ((wcode & 0xff) != kWinGeneric) {
           R = (wcode & 0xff) - 2;
           if (wcode & kWinHasTieOnly) {
@@ -741,13 +754,23 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
         }
 #pragma unroll
         for (int kk = 0; kk < KW; ++kk) {
-          const bool valid = c.t0 + lane + 32 * kk < L;
+          const bool valid = lvalid(kk);
           const bool win = valid && mw[kk] <= msg_g;
           msg[kk] = win ? mw[kk] : msg_g;
           am[kk] = win ? aw[kk] : argmin_h;
           own[kk] = win && mw[kk] < msg_g;
         }
-        if (s1 >= 0) {
+        bool fix = s1 >= 0;
+        if (fix && (wcode & kWinTieIsL2) && s1 == argmin_h) {
+          // s1 is the minimum of h and the tie-only taps are L2: every
+          // tie-only term of s1 equals the candidate, which only changes the
+          // argmin of a label whose beating terms reach exactly the candidate
+          bool eq = false;
+#pragma unroll
+          for (int kk = 0; kk < KW; ++kk) eq = eq || (mw[kk] == msg_g);
+          fix = __any_sync(FULL, eq);
+        }
+        if (fix) {
           // a tie with the candidate at a tie-only offset of s1: the last
           // sender at the candidate value takes the argmin
           const float hs1 = cs.hs[s1];
@@ -757,7 +780,7 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
             const int jd = s1 - t;
             const int ajd = jd < 0 ? -jd : jd;
             const float f = tile[max(1, min(a.Lv - 1, c0 - jd)) * 33 + j];
-            const bool tie = (t < L) && ajd > R && ajd <= delta && __fmaf_rn(f, w, hs1) == msg_g && !(mw[kk] < msg_g);
+            const bool tie = lvalid(kk) && ajd > R && ajd <= delta && __fmaf_rn(f, w, hs1) == msg_g && !(mw[kk] < msg_g);
             am[kk] = tie ? ((mw[kk] == msg_g) ? max(aw[kk], s1) : s1) : am[kk];
           }
         }
@@ -856,7 +879,7 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
         e_g = __shfl_sync(FULL, y, __ffs(~bsel) - 1);
 #pragma unroll
         for (int kk = 0; kk < KW; ++kk) {
-          const bool valid = c.t0 + lane + 32 * kk < L;
+          const bool valid = lvalid(kk);
           e[kk] = own[kk] ? y : (valid ? e_g : 0.0f);
         }
       } else {
@@ -883,7 +906,7 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
           __syncwarp();
 #pragma unroll
           for (int kk = 0; kk < KW; ++kk) {
-            const bool valid = c.t0 + lane + 32 * kk < L;
+            const bool valid = lvalid(kk);
             const float eo = eb[own[kk] ? pos[kk] : 0];
             e[kk] = own[kk] ? eo : (valid ? e_g : 0.0f);
           }
@@ -892,7 +915,7 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
           all_ok = exp_try<kExact>(earg(msg_g), e_g, s_ehi, s_elo);
 #pragma unroll
           for (int kk = 0; kk < KW; ++kk) {
-            const bool valid = c.t0 + lane + 32 * kk < L;
+            const bool valid = lvalid(kk);
             e[kk] = valid ? e_g : 0.0f;
             if (__any_sync(FULL, own[kk])) {
               float ex;
@@ -910,7 +933,7 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
         e_g = static_cast<float>(exp(static_cast<double>(msg_g)));
 #pragma unroll
         for (int kk = 0; kk < KW; ++kk) {
-          const bool valid = c.t0 + lane + 32 * kk < L;
+          const bool valid = lvalid(kk);
           e[kk] = own[kk] ? static_cast<float>(exp(static_cast<double>(msg[kk]))) : (valid ? e_g : 0.0f);
         }
       }
@@ -951,7 +974,7 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
       const int t = c.t0 + lane + 32 * kk;
       const T o = stf<T>(__fsub_rn(msg[kk], lse));
       chain[kk] = ldf<T>(o);  // the stored value, so the chain matches memory
-      if (t < L) dstm[t] = o;
+      if (lvalid(kk)) dstm[t] = o;
     }
     {
       const int64_t ao = c.out_off + qo;
@@ -959,17 +982,17 @@ __global__ void __launch_bounds__(128, OCC) lbp_forward_kernel(FwdArgs a) {
         uint8_t* d = static_cast<uint8_t*>(a.argmin) + ao;
 #pragma unroll
         for (int kk = 0; kk < KW; ++kk)
-          if (c.t0 + lane + 32 * kk < L) d[c.t0 + lane + 32 * kk] = static_cast<uint8_t>(am[kk]);
+          if (lvalid(kk)) d[c.t0 + lane + 32 * kk] = static_cast<uint8_t>(am[kk]);
       } else if (a.argmin_kind == BPL_ARGMIN_U16) {
         uint16_t* d = static_cast<uint16_t*>(a.argmin) + ao;
 #pragma unroll
         for (int kk = 0; kk < KW; ++kk)
-          if (c.t0 + lane + 32 * kk < L) d[c.t0 + lane + 32 * kk] = static_cast<uint16_t>(am[kk]);
+          if (lvalid(kk)) d[c.t0 + lane + 32 * kk] = static_cast<uint16_t>(am[kk]);
       } else if (a.argmin_kind == BPL_ARGMIN_F32) {
         float* d = static_cast<float*>(a.argmin) + ao;
 #pragma unroll
         for (int kk = 0; kk < KW; ++kk)
-          if (c.t0 + lane + 32 * kk < L) d[c.t0 + lane + 32 * kk] = static_cast<float>(am[kk]);
+          if (lvalid(kk)) d[c.t0 + lane + 32 * kk] = static_cast<float>(am[kk]);
       }
     }
     // (float)max((double)sum, 1e-45): the smallest positive float when sum is 0
@@ -1002,16 +1025,21 @@ int launch_phase(const FwdArgs& a, cudaStream_t stream) {
   const int lroww = 32 * (K / NW);
   const size_t per_chain = 4 * (static_cast<size_t>(chain_smem_floats(K)) +
                                 static_cast<size_t>(NW) * warp_smem_floats(a.ns, lroww, a.lmat, a.Lv, sizeof(T)));
-  // chains per block: up to 4 warps while the block fits in 200 KB
-  const int cpb = std::max(1, std::min(4 / NW, static_cast<int>((200 * 1024) / per_chain)));
-  const size_t smem = per_chain * cpb;
-  // a phase with more scanlines than about 8 warps per SM keeps 4 blocks
-  // resident (registers capped at 128); fewer scanlines run latency-bound
-  // and keep every register they use
+  // a phase with more scanlines than about 8 warps per SM runs 1-warp
+  // blocks, kHiOcc resident per SM (registers capped near 120); fewer
+  // scanlines run latency-bound in 4-warp blocks and keep every register
+  // they use
   auto kern = lbp_forward_kernel<K, V, NW, T, 1>;
+  int wmax = 4;
   if constexpr (K <= 8) {
-    if (a.nchains > kHiOccChainsPerSm * sm_count()) kern = lbp_forward_kernel<K, V, NW, T, 4>;
+    if (NW == 1 && a.nchains > kHiOccChainsPerSm * sm_count()) {
+      kern = lbp_forward_kernel<K, V, NW, T, kHiOcc>;
+      wmax = fwd_block_warps<kHiOcc>();
+    }
   }
+  // chains per block: up to wmax warps while the block fits in 200 KB
+  const int cpb = std::max(1, std::min(wmax / NW, static_cast<int>((200 * 1024) / per_chain)));
+  const size_t smem = per_chain * cpb;
   if (smem > 48 * 1024) {
     if (static_cast<int>(smem) > max_smem_optin())
       return set_error(BPL_ERR_UNSUPPORTED, "lbp_forward: shared memory %zu exceeds device limit", smem);
