@@ -17,11 +17,19 @@
 // and grad_messages = in_grad (:534-536).
 //
 // GB300 design: one warp walks one scanline of one backward sweep, the
-// accumulators acc_HOR/UP/DOWN stay in registers, the scatter "by argmin"
-// goes through per-warp shared-memory rows with shared atomics, and the two
-// sweeps of each orientation run concurrently (DOWN+UP, then LEFT+RIGHT):
-// 2 launches per backward instead of 2(W-1)+2(H-1).  The J^T product is taken
-// in O(L) as g_c - p_c * sum(g) instead of the reference's O(L^2) loop.
+// accumulator stays in registers, the scatter "by argmin" goes through a
+// per-warp shared-memory row with shared atomics, and the two sweeps of each
+// orientation run concurrently (DOWN+UP, then LEFT+RIGHT): 2 launches per
+// backward instead of 2(W-1)+2(H-1).  The J^T product is taken in O(L) as
+// g_c - p_c * sum(g) instead of the reference's O(L^2) loop.
+//
+// One accumulator instead of HOR/UP/DOWN.  acc_UP/acc_DOWN are scatters of
+// the saved vertical accumulators, which are themselves scatters of J^T
+// outputs; J^T = I - p 1^T produces vectors that sum to zero and a scatter
+// keeps the sum, so J^T leaves acc_UP + saved_UP unchanged.  Applying J^T
+// to (in_grad + saved_UP + saved_DOWN + acc) in a single accumulator
+// therefore gives the reference's sums, up to float rounding, with a third
+// of the scatter atomics and row traffic.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -180,6 +188,9 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
   }
   const int fd = db ^ 1;
   const bool stereo = (VARIANT == BPL_LBP_STEREO);
+  // label validity: with K = ceil(L/32) (the K <= 8 instantiations are
+  // dispatched exactly) only the last slot can hold labels >= L
+  auto lvalid = [&](int kk) -> bool { return (K <= 8 && kk < K - 1) || (lane + 32 * kk < L); };
   const int nj = (a.jb == 1) ? 0 : n;
   const int ne = (a.eb == 1) ? 0 : n;
   const uint32_t am_size = (a.argmin_kind == BPL_ARGMIN_U8) ? 1u : (a.argmin_kind == BPL_ARGMIN_U16 ? 2u : 4u);
@@ -222,21 +233,21 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
     if (a.argmin_kind == BPL_ARGMIN_U8) {
       const uint8_t* ab = am_db + qo;
 #pragma unroll
-      for (int kk = 0; kk < K; ++kk) pa_[kk] = __ldg(ab + ((lane + 32 * kk < L) ? lane + 32 * kk : 0));
+      for (int kk = 0; kk < K; ++kk) pa_[kk] = __ldg(ab + (lvalid(kk) ? lane + 32 * kk : 0));
     } else if (a.argmin_kind == BPL_ARGMIN_U16) {
       const uint16_t* ab = reinterpret_cast<const uint16_t*>(am_db) + qo;
 #pragma unroll
-      for (int kk = 0; kk < K; ++kk) pa_[kk] = __ldg(ab + ((lane + 32 * kk < L) ? lane + 32 * kk : 0));
+      for (int kk = 0; kk < K; ++kk) pa_[kk] = __ldg(ab + (lvalid(kk) ? lane + 32 * kk : 0));
     } else {
       const float* ab = reinterpret_cast<const float*>(am_db) + qo;
 #pragma unroll
       for (int kk = 0; kk < K; ++kk)
-        pa_[kk] = __float_as_uint(__ldg(ab + ((lane + 32 * kk < L) ? lane + 32 * kk : 0)));
+        pa_[kk] = __float_as_uint(__ldg(ab + (lvalid(kk) ? lane + 32 * kk : 0)));
     }
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const int t = lane + 32 * kk;
-      const int64_t o = qo + ((t < L) ? t : 0);  // labels >= L read label 0 (ignored)
+      const int64_t o = qo + (lvalid(kk) ? t : 0);  // labels >= L read label 0 (ignored)
       pm_[kk] = __ldg(msgs_db + o);
       pg_[kk] = __ldg(grad_db + o);
       if (CROSS) {
@@ -282,12 +293,10 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
   if (nsteps > 32) load_tile_regs(1, rg);
   __syncwarp();
 
-  float accH[K], accU[K], accD[K];
+  float accH[K];
 #pragma unroll
-  for (int k = 0; k < K; ++k) accH[k] = accU[k] = accD[k] = 0.0f;
+  for (int k = 0; k < K; ++k) accH[k] = 0.0f;
   float* rowH = sm.rows;
-  float* rowU = sm.rows + 32 * K;
-  float* rowD = sm.rows + 64 * K;
   const bool am_f32 = a.argmin_kind == BPL_ARGMIN_F32;
 
   int p = pin0;
@@ -298,20 +307,21 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
 
     const float w = tile[a.Lv * 33 + j];
     const float inv_s = (sizeof(T) == 4) ? 1.0f : __frcp_rn(tile[(a.Lv + 1) * 33 + j]);
-    float g[K], pr[K], sU[K], sD[K];
+    float g[K], pr[K];
     int am[K];
     float sg = 0.0f, sa = 0.0f;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
-      const bool valid = lane + 32 * kk < L;
+      const bool valid = lvalid(kk);
       am[kk] = valid ? (am_f32 ? static_cast<int>(__uint_as_float(pa_[kk])) : static_cast<int>(pa_[kk])) : 0;
-      g[kk] = valid ? bldf<T>(pg_[kk]) : 0.0f;
+      // horizontal sweeps: the vertical chains' saved gradients join in_grad
+      // in the one accumulator (see the kernel's comment on the vertical
+      // accumulators)
+      g[kk] = valid ? (CROSS ? (bldf<T>(pg_[kk]) + pu_[kk]) + pd_[kk] : bldf<T>(pg_[kk])) : 0.0f;
       // exp(m + log S) / S of the reference (:328-341) is exp(m) for a
       // normalised message m = m_raw - log S; half rows hold m_raw - min h
       // with their scale the sum of exp of the row, so exp(m) = exp(row) / scale
       pr[kk] = valid ? __expf(bldf<T>(pm_[kk])) * inv_s : 0.0f;
-      sU[kk] = (CROSS && valid) ? pu_[kk] : 0.0f;
-      sD[kk] = (CROSS && valid) ? pd_[kk] : 0.0f;
       sg += g[kk];
       sa += accH[kk];
     }
@@ -332,8 +342,8 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       addH[kk] = (g[kk] - pr[kk] * sg) + (accH[kk] - pr[kk] * sa);
-      addU[kk] = CROSS ? sU[kk] + accU[kk] : 0.0f;
-      addD[kk] = CROSS ? sD[kk] + accD[kk] : 0.0f;
+      addU[kk] = 0.0f;
+      addD[kk] = 0.0f;
     }
 
     // Scatter by argmin.  Most labels share one argmin (the label of the
@@ -349,7 +359,7 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
     int c0 = 0, cL = 0;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
-      const bool v = lane + 32 * kk < L;
+      const bool v = lvalid(kk);
       c0 += (v && am[kk] == g0) ? 1 : 0;
       cL += (v && am[kk] == gL) ? 1 : 0;
     }
@@ -361,22 +371,12 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
     for (int q = 0; q < 8; ++q) dsum[q] = 0.0f;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
-      const bool v = lane + 32 * kk < L;
+      const bool v = lvalid(kk);
       const bool dom = v && am[kk] == gd;
       dsum[0] += dom ? addH[kk] : 0.0f;
-      if (CROSS) {
-        dsum[1] += dom ? addU[kk] : 0.0f;
-        dsum[2] += dom ? addD[kk] : 0.0f;
-      }
       const bool nd = v && !dom;
       if (__any_sync(FULL, nd)) {
-        if (nd) {
-          atomicAdd(&rowH[am[kk]], addH[kk]);
-          if (CROSS) {
-            atomicAdd(&rowU[am[kk]], addU[kk]);
-            atomicAdd(&rowD[am[kk]], addD[kk]);
-          }
-        }
+        if (nd) atomicAdd(&rowH[am[kk]], addH[kk]);
       }
     }
 
@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
 #pragma unroll
       for (int kk = 0; kk < K; ++kk) {
         const int t = lane + 32 * kk;
-        const float tot = (t < L) ? (addH[kk] + addU[kk]) + addD[kk] : 0.0f;
+        const float tot = lvalid(kk) ? (addH[kk] + addU[kk]) + addD[kk] : 0.0f;
         const int ti = max(1, min(lv - 1, lv / 2 + (t - am[kk])));
 #pragma unroll
         for (int bb = 1; bb < NB; ++bb)
@@ -411,13 +411,9 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
           if (r != 0.0f) atomicAdd(gjump_fd + static_cast<int64_t>(bb) * HW + p, w * r);
         }
         if (lane == 0) rowH[gd] += r;  // no other lane touches label gd
-        if (CROSS && lane == 4) rowU[gd] += r;
-        if (CROSS && lane == 8) rowD[gd] += r;
       } else {
         const float r = warp_reduce_scatter8(dsum, lane);
         if (lane == 0) rowH[gd] += r;
-        if (CROSS && lane == 4) rowU[gd] += r;
-        if (CROSS && lane == 8) rowD[gd] += r;
         // taps 1..NB-1 in passes of 8
 #pragma unroll
         for (int b0 = 0; b0 < NB; b0 += 8) {
@@ -437,8 +433,6 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
     } else {
       const float r = warp_reduce_scatter8(dsum, lane);
       if (lane == 0) rowH[gd] += r;
-      if (CROSS && lane == 4) rowU[gd] += r;
-      if (CROSS && lane == 8) rowD[gd] += r;
 #pragma unroll
       for (int kk = 0; kk < K; ++kk) {
         const int t = lane + 32 * kk;
@@ -462,7 +456,7 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
     __syncwarp();
 
     // read back the chain accumulators (and clear the rows for the next
-    // step); grad_cost[p][s] receives rowH + rowU + rowD.  The rows are 32K
+    // step); grad_cost[p][s] receives the row.  The rows are 32K
     // long, so labels >= L read zeros.
     float* gc = gcost_n + static_cast<int64_t>(p) * Ls;
 #pragma unroll
@@ -470,17 +464,10 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
       const int t = lane + 32 * kk;
       accH[kk] = rowH[t];
       rowH[t] = 0.0f;
-      float v = accH[kk];
-      if (CROSS) {
-        accU[kk] = rowU[t];
-        accD[kk] = rowD[t];
-        rowU[t] = 0.0f;
-        rowD[t] = 0.0f;
-        v = (v + accU[kk]) + accD[kk];
-      }
-      if (t < L && v != 0.0f) atomicAdd(gc + t, v);
-      if (!CROSS && t < L) saved_out[static_cast<int64_t>(p) * Ls + t] = accH[kk];
-      if (CROSS && a.gmsg != nullptr && t < L) {
+      const float v = accH[kk];
+      if (lvalid(kk) && v != 0.0f) atomicAdd(gc + t, v);
+      if (!CROSS && lvalid(kk)) saved_out[static_cast<int64_t>(p) * Ls + t] = accH[kk];
+      if (CROSS && a.gmsg != nullptr && lvalid(kk)) {
         float* gm = a.gmsg + static_cast<int64_t>(n) * 4 * HWL;
         if (v != 0.0f) atomicAdd(gm + UP * HWL + static_cast<int64_t>(p) * Ls + t, v);
         if (k == nsteps - 1) gm[db * HWL + static_cast<int64_t>(p) * Ls + t] = v;
