@@ -109,27 +109,51 @@ class LBPMinSumFunction(torch.autograd.Function):
     returns in_grad as the message gradient.  adjoint "exact": the
     derivative of the forward; each pass keeps a copy of its own output
     messages and returns the gradient with respect to its input messages,
-    so chained passes differentiate exactly."""
+    so chained passes differentiate exactly.
+
+    recompute=True stores no argmin indices: the pass keeps a copy of its
+    input messages instead and its backward re-runs the pass on a copy of
+    them, each warp regenerating its scanline's indices into a scratch
+    buffer (bit-identical: the same kernel on the same inputs), before the
+    adjoint.  Trades one forward pass of work in backward for the index
+    tensor (L bytes per pixel and direction) of every pass."""
 
     @staticmethod
-    def forward(ctx, cost, edge, messages, delta, affinities, offset, adjoint="reference"):
+    def forward(ctx, cost, edge, messages, delta, affinities, offset, adjoint="reference", recompute=False):
         taps = pack_affinities(affinities, offset)
         L = cost.shape[-1]
         am_dtype = torch.uint8 if L <= 256 else torch.int16
+        ctx.adjoint = adjoint
+        ctx.recompute = recompute
+        ctx.delta = int(delta)
+        ctx.am_dtype = am_dtype
+        if recompute:
+            m_in = messages.detach().clone()
+            messages, _, scale = ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta),
+                                                 argmin_dtype=None)
+            own = messages.clone() if adjoint == "exact" else messages
+            ctx.save_for_backward(cost, taps, edge, own, m_in, scale)
+            return messages
         messages, argmin, scale = ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta),
                                                   argmin_dtype=am_dtype)
-        ctx.adjoint = adjoint
         own = messages.clone() if adjoint == "exact" else messages
         ctx.save_for_backward(cost, taps, edge, own, argmin, scale)
         return messages
 
     @staticmethod
     def backward(ctx, in_grad):
-        cost, taps, edge, messages, argmin, scale = ctx.saved_tensors
+        cost, taps, edge, messages, saved, scale = ctx.saved_tensors
+        if ctx.recompute:
+            # the pass again, on a copy of its input: its argmin indices
+            # (the messages and scales it writes equal the saved ones)
+            _, argmin, _ = ops.lbp_forward(ops.LBP_STEREO, cost.detach(), taps, edge, saved.clone(), ctx.delta,
+                                           argmin_dtype=ctx.am_dtype)
+        else:
+            argmin = saved
         gc, gtaps, ge, gm = ops.lbp_backward(ops.LBP_STEREO, taps, edge, in_grad.contiguous(), messages, argmin,
                                              scale, copy_grad_messages=False, mode=ctx.adjoint)
         g_aff, g_off = unpack_affinity_grad(gtaps)
-        return gc, ge, gm, None, g_aff, g_off, None
+        return gc, ge, gm, None, g_aff, g_off, None, None
 
 
 class LBPMinSumFunctionF16(torch.autograd.Function):
@@ -227,7 +251,8 @@ class MessagePassing(nn.Module):
         elif value_L1 > value_L2:
             raise ValueError("L1 must be smaller than or equal L2!")
 
-    def __init__(self, device, max_iter, num_labels, delta, mode="min-sum", storage="fp32", adjoint="reference"):
+    def __init__(self, device, max_iter, num_labels, delta, mode="min-sum", storage="fp32", adjoint="reference",
+                 recompute_argmin=False):
         super().__init__()
         self.device = device
         self.max_iter = max_iter
@@ -239,7 +264,10 @@ class MessagePassing(nn.Module):
             raise ValueError("adjoint must be reference or exact")
         if adjoint == "exact" and storage != "fp32":
             raise ValueError("the exact adjoint runs with fp32 storage")
+        if recompute_argmin and storage != "fp32":
+            raise ValueError("argmin recomputation runs with fp32 storage")
         self.adjoint = adjoint
+        self.recompute_argmin = recompute_argmin
         self.mode = mode
         self.storage = storage
         self._L1 = nn.Parameter(torch.tensor(0.1, device=device), requires_grad=True)
@@ -277,13 +305,13 @@ class MessagePassing(nn.Module):
             messages = LBPMinSumLoop.apply(cost, cost_h, edge_weights, messages, self.delta, affinities, offset,
                                            self.max_iter)
             return BeliefsSoftmin.apply(messages, cost, self.softmin.T), messages
-        if self.adjoint == "reference":
+        if self.adjoint == "reference" and not self.recompute_argmin:
             messages = LBPMinSumLoop.apply(cost, None, edge_weights, messages, self.delta, affinities, offset,
                                            self.max_iter)
         else:
             for _ in range(self.max_iter):
                 messages = LBPMinSumFunction.apply(cost, edge_weights, messages, self.delta, affinities, offset,
-                                                   self.adjoint)
+                                                   self.adjoint, self.recompute_argmin)
         return BeliefsSoftmin.apply(messages, cost, self.softmin.T), messages
 
 

@@ -83,3 +83,35 @@ def test_message_passing_exact_adjoint_through_iterations():
     assert abs(mp._L2.grad.item() - gL2) <= 2e-4 * max(abs(gL2), 1.0)
     # the initial messages' gradient is the first pass's input-message gradient
     np.testing.assert_allclose(m0.grad.detach().cpu().numpy(), G, atol=2e-4 * max(1.0, np.abs(G).max()))
+
+
+@pytest.mark.parametrize("adjoint", ["reference", "exact"])
+def test_recompute_argmin_variant_matches_stored(adjoint):
+    """MessagePassing(recompute_argmin=True) stores no indices and
+    regenerates them per scanline in backward: gradients equal those of the
+    index-storing variant (config: B=4, per-pixel edge weights U[0.5,2],
+    reduced from 256x512x96 to keep the test short)."""
+    from bpl_gb300.layers.stereo import MessagePassing
+    dev = torch.device("cuda:0")
+    g = cases.rng(23)
+    B, H, W, L, iters = 4, 32, 64, 96, 3
+    prob = torch.from_numpy(cases.softmax_np(g.normal(0, 2, size=(B, H, W, L)).astype(np.float32))).to(dev)
+    edge = torch.from_numpy(g.uniform(0.5, 2.0, size=(B, 4, H, W)).astype(np.float32)).to(dev)
+    up = torch.randn((B, H, W, L), device=dev, generator=torch.Generator(device=dev).manual_seed(2))
+    grads = []
+    for rec in (False, True):
+        mp = MessagePassing(dev, iters, L, 3, adjoint=adjoint, recompute_argmin=rec)
+        with torch.no_grad():
+            mp._L1.fill_(0.1)
+            mp._L2.fill_(0.5)
+        p = prob.clone().requires_grad_(True)
+        e = edge.clone().requires_grad_(True)
+        beliefs, _ = mp(p, e, None, None, torch.zeros((B, 4, H, W, L), device=dev, requires_grad=True))
+        beliefs.backward(up)
+        grads.append((beliefs.detach(), p.grad, e.grad, mp._L1.grad.item(), mp._L2.grad.item()))
+    (b0, gp0, ge0, l10, l20), (b1, gp1, ge1, l11, l21) = grads
+    assert torch.equal(b0, b1)
+    assert (gp0 - gp1).abs().max().item() <= 1e-5 * max(1.0, gp0.abs().max().item())
+    assert (ge0 - ge1).abs().max().item() <= 1e-5 * max(1.0, ge0.abs().max().item())
+    assert abs(l10 - l11) <= 1e-5 * max(1.0, abs(l10))
+    assert abs(l20 - l21) <= 1e-5 * max(1.0, abs(l20))
