@@ -218,8 +218,10 @@ class LBPMinSumLoop(torch.autograd.Function):
     @staticmethod
     def backward(ctx, in_grad):
         taps, edge, messages, argmins, scales = ctx.saved_tensors
-        gc, gtaps, ge = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, in_grad.contiguous(), messages,
-                                                argmins, scales, L=ctx.L)
+        # in_grad as autograd hands it over: the beliefs' gradient expanded over
+        # the four slots is read in place (slot stride 0), not materialised
+        gc, gtaps, ge = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, in_grad, messages, argmins, scales,
+                                                L=ctx.L)
         g_aff, g_off = unpack_affinity_grad(gtaps)
         if ctx.half:
             gc = gc[..., :ctx.L]
