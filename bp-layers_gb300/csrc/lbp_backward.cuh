@@ -356,28 +356,37 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
       if (kk == ((L - 1) >> 5)) amL = am[kk];
     const int g0 = __shfl_sync(FULL, am[0], 0);
     const int gL = __shfl_sync(FULL, amL, (L - 1) & 31);
-    int c0 = 0, cL = 0;
+    // the dominant group: the first and last labels' shared argmin (labels
+    // far from the window winners take the global minimum's label), else the
+    // larger of their two groups
+    int gd = g0;
+    if (g0 != gL) {
+      int c0 = 0, cL = 0;
 #pragma unroll
-    for (int kk = 0; kk < K; ++kk) {
-      const bool v = lvalid(kk);
-      c0 += (v && am[kk] == g0) ? 1 : 0;
-      cL += (v && am[kk] == gL) ? 1 : 0;
+      for (int kk = 0; kk < K; ++kk) {
+        const bool v = lvalid(kk);
+        c0 += (v && am[kk] == g0) ? 1 : 0;
+        cL += (v && am[kk] == gL) ? 1 : 0;
+      }
+      c0 = __reduce_add_sync(FULL, c0);
+      cL = __reduce_add_sync(FULL, cL);
+      gd = (c0 >= cL) ? g0 : gL;
     }
-    c0 = __reduce_add_sync(FULL, c0);
-    cL = __reduce_add_sync(FULL, cL);
-    const int gd = (c0 >= cL) ? g0 : gL;
     float dsum[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) dsum[q] = 0.0f;
+    bool any_nd = false;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const bool v = lvalid(kk);
       const bool dom = v && am[kk] == gd;
       dsum[0] += dom ? addH[kk] : 0.0f;
-      const bool nd = v && !dom;
-      if (__any_sync(FULL, nd)) {
-        if (nd) atomicAdd(&rowH[am[kk]], addH[kk]);
-      }
+      any_nd = any_nd || (v && !dom);
+    }
+    if (__any_sync(FULL, any_nd)) {
+#pragma unroll
+      for (int kk = 0; kk < K; ++kk)
+        if (lvalid(kk) && am[kk] != gd) atomicAdd(&rowH[am[kk]], addH[kk]);
     }
 
     // pairwise and edge gradients: per-tap sums of the total contribution,
