@@ -13,8 +13,10 @@
 // accumulates a 4-pixel x 8-disparity register tile over the channels in
 // order (two FP32 instructions per term, no FMA: bit-identical to the
 // reference), then writes its 8 disparities of each pixel as two 16-byte
-// stores.  FP32-issue bound (about 29 flop/byte at 376x1240x64x192), so no
-// TMA pipeline: one staged tile per block.
+// stores.  FP32-issue bound (about 29 flop/byte at 376x1240x64x192); the
+// channel chunks are double-buffered (cp.async of chunk i+1 while chunk i is
+// summed), because a 512-thread block leaves one block per SM and a
+// synchronous load per chunk stalled the whole SM.
 // Backward: one thread per (channel, pixel) walks the disparities in the
 // reference order (additions of +-g in the same sequence: bit-identical); the
 // upstream-gradient rows are shared through L1 by the block's channels.
@@ -50,21 +52,32 @@ __device__ __forceinline__ int disparity(const SadArgs& a, int di) {
   return static_cast<int>(__fadd_rn(__fmul_rn(static_cast<float>(di), a.step), static_cast<float>(a.min_disp)));
 }
 
-// grid (ceil(W/kTX), H, B); block (D/kPD rounded up) x (kTX/kPX) threads
+// Shared-memory layout and lane mapping: lanes take consecutive pixel groups
+// (16 per disparity group) so a quarter-warp's reads of its f1 windows are
+// consecutive 16-byte chunks; each f1 row is staged with a leading pad that
+// makes every thread's 11-value window start 16-byte aligned (three 128-bit
+// loads, conflict-free).  With lanes on consecutive disparity groups the
+// windows were 8 floats apart: an 8-way bank conflict.
+constexpr int kPXG = kTX / kPX;  // pixel groups per block
+
+// leading pad of an f1 row: (window start + pad) % 4 == 0 for every thread
+__host__ __device__ inline int sad_pad(int dhi, int dlo) { return ((7 - (dhi - dlo)) % 4 + 4) % 4; }
+
+// grid (ceil(W/kTX), H, B); block kPXG x (D/kPD rounded up) threads
 __global__ void __launch_bounds__(512) sad_forward_kernel(SadArgs a) {
   extern __shared__ __align__(16) float sm[];
   const int n = blockIdx.z, y = blockIdx.y, x0 = blockIdx.x * kTX;
   const int span = kTX + (a.dhi - a.dlo);      // f1 columns a block can match
-  const int spanp = (span + 3) & ~3;
-  float* s0 = sm;                              // [kCChunk][kTX]
-  float* s1 = sm + kCChunk * kTX;              // [kCChunk][spanp]
-  const int xb = x0 - a.dhi;                   // f1 column of s1[.][0]
+  const int pad = a.unit_step ? sad_pad(a.dhi, a.dlo) : 0;
+  const int spanp = (pad + span + 3) & ~3;
+  const int bufsz = kCChunk * (kTX + spanp);   // one chunk: s0 [kCChunk][kTX], s1 [kCChunk][spanp]
+  const int xb = x0 - a.dhi - pad;             // f1 column of s1[.][0]
   const int ndg = (a.D + kPD - 1) / kPD;
   const int tid = threadIdx.x;
   const int nthreads = blockDim.x;
-  const int dg = tid % ndg;                    // disparity group
-  const int xg = tid / ndg;                    // pixel group
-  const bool active = xg < kTX / kPX;
+  const int xg = tid % kPXG;                   // pixel group
+  const int dg = tid / kPXG;                   // disparity group
+  const bool active = dg < ndg;
   const int64_t HW = static_cast<int64_t>(a.H) * a.W;
   const float* f0 = a.f0 + static_cast<int64_t>(n) * a.C * HW + static_cast<int64_t>(y) * a.W;
   const float* f1 = a.f1 + static_cast<int64_t>(n) * a.C * HW + static_cast<int64_t>(y) * a.W;
@@ -78,33 +91,60 @@ __global__ void __launch_bounds__(512) sad_forward_kernel(SadArgs a) {
 #pragma unroll
     for (int q = 0; q < kPD; ++q) acc[p][q] = 0.0f;
 
-  for (int c0 = 0; c0 < a.C; c0 += kCChunk) {
+  // stage chunk `ci` into buffer ci & 1 (cp.async; zeros outside the image)
+  auto stage = [&](int ci) {
+    const int c0 = ci * kCChunk;
     const int cn = min(kCChunk, a.C - c0);
-    __syncthreads();
+    float* s0 = sm + (ci & 1) * bufsz;
+    float* s1 = s0 + kCChunk * kTX;
     for (int e = tid; e < cn * kTX; e += nthreads) {
       const int cc = e / kTX, xx = e % kTX, x = x0 + xx;
-      s0[cc * kTX + xx] = (x < a.W) ? f0[(c0 + cc) * HW + x] : 0.0f;
+      if (x < a.W) cp_async4(s0 + cc * kTX + xx, f0 + (c0 + cc) * HW + x);
+      else s0[cc * kTX + xx] = 0.0f;
     }
     for (int e = tid; e < cn * spanp; e += nthreads) {
       const int cc = e / spanp, xx = e % spanp, x = xb + xx;
-      s1[cc * spanp + xx] = (x >= 0 && x < a.W && xx < span) ? f1[(c0 + cc) * HW + x] : 0.0f;
+      if (x >= 0 && x < a.W && xx >= pad && xx < pad + span) cp_async4(s1 + cc * spanp + xx, f1 + (c0 + cc) * HW + x);
+      else s1[cc * spanp + xx] = 0.0f;
+    }
+    cp_async_commit();
+  };
+  const int nchunk = (a.C + kCChunk - 1) / kCChunk;
+  stage(0);
+  for (int ci = 0; ci < nchunk; ++ci) {
+    const int c0 = ci * kCChunk;
+    const int cn = min(kCChunk, a.C - c0);
+    if (ci + 1 < nchunk) {
+      stage(ci + 1);
+      cp_async_wait<1>();  // chunk ci has landed (ci + 1 may be in flight)
+    } else {
+      cp_async_wait<0>();
     }
     __syncthreads();
+    const float* s0 = sm + (ci & 1) * bufsz;
+    const float* s1 = s0 + kCChunk * kTX;
     if (active) {
       for (int cc = 0; cc < cn; ++cc) {
         float v0[kPX];
-#pragma unroll
-        for (int p = 0; p < kPX; ++p) v0[p] = s0[cc * kTX + xg * kPX + p];
+        {
+          const float4 q0 = *reinterpret_cast<const float4*>(s0 + cc * kTX + xg * kPX);
+          v0[0] = q0.x; v0[1] = q0.y; v0[2] = q0.z; v0[3] = q0.w;
+        }
         const float* r1 = s1 + cc * spanp;
-        // f1 column x - d sits at s1 index xl + dhi - d (xl: pixel in block)
+        // f1 column x - d sits at s1 index xl + pad + dhi - d (xl: pixel in block)
         if (a.unit_step) {
-          // d = d0 + q: the 4 x 8 tile reads 11 consecutive f1 values
-          // (indices below 0 of the last, partial disparity group land in
-          // the f0 tile and feed only outputs that are not stored)
-          const int base = xg * kPX + a.dhi - dv[0];
-          float v1[kPX + kPD - 1];
+          // d = d0 + q: the 4 x 8 tile reads 11 consecutive f1 values, from a
+          // 16-byte aligned start (indices below 0 of the last, partial
+          // disparity group land in the f0 tile and feed only outputs that
+          // are not stored)
+          const int base = xg * kPX + pad + a.dhi - dv[0];
+          float v1[kPX + kPD + 1];
+          const float4* q1 = reinterpret_cast<const float4*>(r1 + base - (kPD - 1));
 #pragma unroll
-          for (int k = 0; k < kPX + kPD - 1; ++k) v1[k] = r1[base - (kPD - 1) + k];
+          for (int k = 0; k < 3; ++k) {
+            const float4 t = q1[k];
+            v1[4 * k] = t.x; v1[4 * k + 1] = t.y; v1[4 * k + 2] = t.z; v1[4 * k + 3] = t.w;
+          }
 #pragma unroll
           for (int p = 0; p < kPX; ++p)
 #pragma unroll
@@ -116,13 +156,14 @@ __global__ void __launch_bounds__(512) sad_forward_kernel(SadArgs a) {
             const int xl = xg * kPX + p;
 #pragma unroll
             for (int q = 0; q < kPD; ++q) {
-              const float v1 = r1[xl + a.dhi - dv[q]];
+              const float v1 = r1[xl + pad + a.dhi - dv[q]];
               acc[p][q] = __fadd_rn(acc[p][q], fabsf(__fsub_rn(v0[p], v1)));
             }
           }
         }
       }
     }
+    __syncthreads();  // buffer ci & 1 is restaged by the next iteration's stage(ci + 2)
   }
   if (!active) return;
   float* out = a.out + ((static_cast<int64_t>(n) * a.H + y) * a.W) * a.D;
@@ -224,10 +265,11 @@ extern "C" int bpl_sad_forward(const float* f0, const float* f1, float* out, int
   a.dhi = a.unit_step ? hi : hi + 1;
   BPL_REQUIRE(a.dhi - a.dlo <= 4096, "sad_forward: disparity span %d too large", a.dhi - a.dlo);
   const int ndg = (D + kPD - 1) / kPD;
-  const int threads = ndg * (kTX / kPX);
+  const int threads = ndg * kPXG;
   BPL_REQUIRE(threads <= 1024, "sad_forward: D=%d too large (at most %d disparities)", D, 1024 / (kTX / kPX) * kPD);
   const int span = kTX + (a.dhi - a.dlo);
-  const size_t smem = sizeof(float) * kCChunk * (kTX + ((span + 3) & ~3));
+  const int pad = a.unit_step ? sad_pad(a.dhi, a.dlo) : 0;
+  const size_t smem = 2 * sizeof(float) * kCChunk * (kTX + ((pad + span + 3) & ~3));  // two chunk buffers
   if (smem > 48 * 1024) {
     BPL_REQUIRE(static_cast<int>(smem) <= max_smem_optin(), "sad_forward: disparity span too large");
     BPL_CUDA_TRY(cudaFuncSetAttribute(sad_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
