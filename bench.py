@@ -444,10 +444,12 @@ def run_reference(args):
 
 
 def run_ncu_case(args):
-    """Small case for detailed ncu captures: the second of two forward passes
-    and reference-adjoint passes at 256x512x192 on the synthetic scene (cost
-    100 MB, messages 400 MB: larger than L2, well under the capture size
-    limit), inside a profiler range."""
+    """Small cases for detailed ncu captures, inside a profiler range (the
+    second run of each): LBP forward and reference adjoint at 256x512x192
+    (cost 100 MB, messages 400 MB: larger than L2, well under the capture
+    size limit), the exact adjoint's message-gradient assembly, the belief
+    epilogue, SAD at 384x512 C=64 D=192 and the flow SAD at 384x512 C=32,
+    window +-32."""
     import torch
     from bpl_gb300 import ops
     import cases
@@ -458,12 +460,24 @@ def run_ncu_case(args):
     jump = torch.from_numpy(cases.stereo_taps(1, h, w, 0.1, 0.5)).to(dev)
     gin = torch.randn((1, 4, h, w, L), device=dev)
     m = torch.zeros((1, 4, h, w, L), device=dev)
+    T = torch.ones(1, device=dev)
+    f0 = torch.randn((1, 64, 384, 512), device=dev)
+    f1 = torch.randn((1, 64, 384, 512), device=dev)
+    g0 = torch.randn((1, 32, 384, 512), device=dev)
+    g1 = torch.randn((1, 32, 384, 512), device=dev)
     for it in range(2):
         if it == 1:
             torch.cuda.synchronize()
             torch.cuda.profiler.start()
         m, am, sc = ops.lbp_forward(ops.LBP_STEREO, cost, jump, edge, m, DELTA, argmin_dtype=torch.uint8)
         ops.lbp_backward(ops.LBP_STEREO, jump, edge, gin, m, am, sc, copy_grad_messages=False)
+        ops.lbp_backward(ops.LBP_STEREO, jump, edge, gin, m, am, sc, mode="exact")
+        b = ops.beliefs_forward(m, cost, T)
+        ops.beliefs_backward(m, cost, T, b, prob)
+        vol = ops.sad_forward(f0, f1, 0, L - 1)
+        ops.sad_backward(f0, f1, 0, L - 1, vol)
+        cu, cv, us, vs = ops.flow_forward(g0, g1, 64)
+        ops.flow_backward(g0, g1, 64, cu, cv, us, vs)
         torch.cuda.synchronize()
     torch.cuda.profiler.stop()
     print(json.dumps({"ncu_case": f"{h}x{w}x{L}", "updates_per_pass": L * edges(h, w)}))
