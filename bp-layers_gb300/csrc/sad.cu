@@ -19,7 +19,9 @@
 // synchronous load per chunk stalled the whole SM.
 // Backward: one thread per (channel, pixel) walks the disparities in the
 // reference order (additions of +-g in the same sequence: bit-identical); the
-// upstream-gradient rows are shared through L1 by the block's channels.
+// upstream gradient is staged per chunk of disparities in shared memory,
+// shared by the block's 16 channels (read directly, a warp's lanes were D
+// floats apart: one sector per lane and load).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -199,37 +201,67 @@ struct SadBwdArgs {
   int channel_limit;
 };
 
-constexpr int kBX = 32;  // pixels per block (backward)
+constexpr int kBX = 32;   // pixels per block (backward)
+constexpr int kBC = 16;   // channels per block
+constexpr int kBD = 32;   // disparities per staged chunk
+constexpr int kBS = kBD + 1;  // padded row stride of the staged chunks
 
-// grid (ceil(W/kBX), H, B*ceil(C/cpb)); block kBX x cpb threads.  The
-// upstream-gradient rows are read through the L1 cache, shared by the
-// block's channels.
-__global__ void __launch_bounds__(256) sad_backward_kernel(SadBwdArgs a, int cpb) {
-  const int ncb = (a.C + cpb - 1) / cpb;
+// grid (ceil(W/kBX), H, B*ceil(C/kBC)); block kBX x kBC threads, one per
+// (channel, pixel), each summing over the disparities in the reference's
+// order.  The upstream gradient is staged per chunk of kBD disparities,
+// shared by the block's channels: gA[px][dd] = g[y, x0+px, d0+dd] (df0) and
+// the diagonal band gD[s][dd] = g[y, x0+d0+s, d0+dd] (df1 reads s = px+dd),
+// rows padded to kBS floats so a warp's reads fall in distinct banks.
+__global__ void __launch_bounds__(kBX * kBC) sad_backward_kernel(SadBwdArgs a) {
+  __shared__ float gA[kBX * kBS];
+  __shared__ float gD[(kBX + kBD - 1) * kBS];
+  const int ncb = (a.C + kBC - 1) / kBC;
   const int n = blockIdx.z / ncb;
-  const int c = (blockIdx.z % ncb) * cpb + threadIdx.y;
+  const int c = (blockIdx.z % ncb) * kBC + threadIdx.y;
   const int y = blockIdx.y;
-  const int x = blockIdx.x * kBX + threadIdx.x;
-  if (x >= a.W || c >= a.C || c >= a.channel_limit) return;
+  const int x0 = blockIdx.x * kBX;
+  const int x = x0 + threadIdx.x;
+  const int tid = threadIdx.y * kBX + threadIdx.x;
+  const bool act = x < a.W && c < a.C && c < a.channel_limit;
   const int64_t HW = static_cast<int64_t>(a.H) * a.W;
   const float* grow = a.g + ((static_cast<int64_t>(n) * a.H + y) * a.W) * a.D;
-  const float* r0 = a.f0 + (static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W;
-  const float* r1 = a.f1 + (static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W;
-  const float a0 = r0[x], b0 = r1[x];
+  const int cc = act ? c : 0;
+  const float* r0 = a.f0 + (static_cast<int64_t>(n) * a.C + cc) * HW + static_cast<int64_t>(y) * a.W;
+  const float* r1 = a.f1 + (static_cast<int64_t>(n) * a.C + cc) * HW + static_cast<int64_t>(y) * a.W;
+  const float a0 = act ? r0[x] : 0.0f, b0 = act ? r1[x] : 0.0f;
   float g0 = 0.0f, g1 = 0.0f;
-  for (int d = a.min_disp; d <= a.max_disp; ++d) {
-    const int idx = d - a.min_disp;
-    if (x - d >= 0 && x - d < a.W) {
-      const float diff = __fsub_rn(a0, __ldg(r1 + x - d));
-      const float gv = __ldg(grow + static_cast<int64_t>(x) * a.D + idx);
-      if (fabsf(diff) > 1e-15f) g0 = (diff > 0.0f) ? __fadd_rn(g0, gv) : __fsub_rn(g0, gv);
+  for (int d0 = a.min_disp; d0 <= a.max_disp; d0 += kBD) {
+    const int i0 = d0 - a.min_disp;  // volume index of d0
+    const int nd = min(kBD, a.max_disp - d0 + 1);
+    __syncthreads();
+    for (int e = tid; e < kBX * kBD; e += kBX * kBC) {
+      const int px = e / kBD, dd = e % kBD, xx = x0 + px;
+      gA[px * kBS + dd] = (xx < a.W && dd < nd) ? __ldg(grow + static_cast<int64_t>(xx) * a.D + i0 + dd) : 0.0f;
     }
-    if (x + d >= 0 && x + d < a.W) {
-      const float diff1 = __fsub_rn(__ldg(r0 + x + d), b0);
-      const float gv = __ldg(grow + static_cast<int64_t>(x + d) * a.D + idx);
-      if (fabsf(diff1) > 1e-15f) g1 = (diff1 > 0.0f) ? __fsub_rn(g1, gv) : __fadd_rn(g1, gv);
+    for (int e = tid; e < (kBX + kBD - 1) * kBD; e += kBX * kBC) {
+      const int sr = e / kBD, dd = e % kBD, xx = x0 + d0 + sr;
+      gD[sr * kBS + dd] =
+          (xx >= 0 && xx < a.W && dd < nd) ? __ldg(grow + static_cast<int64_t>(xx) * a.D + i0 + dd) : 0.0f;
+    }
+    __syncthreads();
+    if (act) {
+      for (int dd = 0; dd < nd; ++dd) {
+        const int d = d0 + dd;
+        if (x - d >= 0 && x - d < a.W) {
+          const float diff = __fsub_rn(a0, __ldg(r1 + x - d));
+          const float gv = gA[threadIdx.x * kBS + dd];
+          if (fabsf(diff) > 1e-15f) g0 = (diff > 0.0f) ? __fadd_rn(g0, gv) : __fsub_rn(g0, gv);
+        }
+        if (x + d >= 0 && x + d < a.W) {
+          const float diff1 = __fsub_rn(__ldg(r0 + x + d), b0);
+          // g[y, x+d, d]: band row (x - x0) + dd (requires x + d = x0 + d0 + row)
+          const float gv = gD[(threadIdx.x + dd) * kBS + dd];
+          if (fabsf(diff1) > 1e-15f) g1 = (diff1 > 0.0f) ? __fsub_rn(g1, gv) : __fadd_rn(g1, gv);
+        }
+      }
     }
   }
+  if (!act) return;
   a.df0[(static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W + x] = g0;
   a.df1[(static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W + x] = g1;
 }
@@ -290,11 +322,10 @@ extern "C" int bpl_sad_backward(const float* f0, const float* f1, const float* i
   SadBwdArgs a{f0, f1, in_grad, df0, df1, B, C, H, W, D, min_disp, max_disp, C};
   // the reference launch covers only 4*ceil(D/4) channels (stereo_sad_kernel.cu:152-157)
   if (reference_channel_limit) a.channel_limit = std::min(C, 4 * ((D + 3) / 4));
-  const int cpb = std::min(8, C);
   BPL_CUDA_TRY(cudaMemsetAsync(df0, 0, sizeof(float) * B * C * H * W, as_stream(stream)), "sad_backward: memset");
   BPL_CUDA_TRY(cudaMemsetAsync(df1, 0, sizeof(float) * B * C * H * W, as_stream(stream)), "sad_backward: memset");
-  dim3 grid((W + kBX - 1) / kBX, H, B * ((C + cpb - 1) / cpb));
-  sad_backward_kernel<<<grid, dim3(kBX, cpb), 0, as_stream(stream)>>>(a, cpb);
+  dim3 grid((W + kBX - 1) / kBX, H, B * ((C + kBC - 1) / kBC));
+  sad_backward_kernel<<<grid, dim3(kBX, kBC), 0, as_stream(stream)>>>(a);
   BPL_CUDA_TRY(cudaGetLastError(), "sad_backward launch");
   return BPL_OK;
 }
