@@ -301,6 +301,8 @@ def run_ours(args):
     }
     if world == 1 and not args.no_serving:
         result["serving"] = run_serving(args)
+    if rank == 0 and world == 1 and not args.no_accuracy:
+        result["accuracy_vs_fp64_oracle"] = run_accuracy()
     traffic = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic):
         with open(traffic) as fh:
@@ -375,6 +377,83 @@ def run_serving(args):
                                 if served["requests_per_s"] and plain["requests_per_s"] else None),
         "slot_plan": {f"{s[0]}x{s[1]}x{s[2]}": {"sets": v[0], "batch": v[1]} for s, v in plan.items()},
     }
+
+
+def _softmin64(z):
+    import numpy as np
+    z = z.astype(np.float64)
+    e = np.exp(-(z - z.min(-1, keepdims=True)))
+    return e / e.sum(-1, keepdims=True)
+
+
+def run_accuracy():
+    """Argmin disagreement and belief max-abs error against the FP64 oracle,
+    per configuration, for FP32 and FP16 storage (beliefs = softmin of the
+    message sum plus cost; argmin = the per-pixel label).  Bounded CPU time:
+    the full-size stereo case is a 376x310 crop, the semantic case a 256x512
+    crop of each of its 2 images."""
+    import numpy as np
+    import torch
+    from bpl_gb300 import ops
+    import cases
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    out = {}
+
+    def report(name, cost, jump_fp32, jump_f16, edge, delta, iters, variant, L):
+        B, H, W, _ = cost.shape
+        m64, _, _ = oracle.lbp_forward(variant, cost.astype(np.float64), jump_fp32, edge,
+                                       np.zeros((B, 4, H, W, L)), delta, fp64=True, iters=iters, threads=0)
+        b64 = _softmin64(m64.sum(1) + cost)
+        lab64 = b64.argmax(-1)
+        res = {}
+        # FP32 storage
+        m = torch.zeros((B, 4, H, W, L), device=dev)
+        for _ in range(iters):
+            ops.lbp_forward(variant, t(cost), t(jump_fp32), t(edge), m, delta, argmin_dtype=None)
+        b = _softmin64(m.cpu().numpy().sum(1) + cost)
+        res["fp32"] = {"argmin_disagreement": float((b.argmax(-1) != lab64).mean()),
+                       "belief_max_abs_error": float(np.abs(b - b64).max())}
+        # FP16 storage (same half-rounded cost for the oracle would isolate the
+        # storage of messages; here the cost is rounded too, as the FP16 layer does)
+        Lp = ops.padded_labels(L)
+        ch = ops.to_half_padded(t(cost), L)
+        mh = torch.zeros((B, 4, H, W, Lp), dtype=torch.float16, device=dev)
+        jh = t(jump_fp32) if variant == 0 else ops.to_half_padded(t(jump_f16), L)
+        for _ in range(iters):
+            ops.lbp_forward_f16(variant, ch, jh, t(edge), mh, delta, L, argmin_dtype=None)
+        b = _softmin64(mh[..., :L].float().cpu().numpy().sum(1) + cost)
+        res["fp16"] = {"argmin_disagreement": float((b.argmax(-1) != lab64).mean()),
+                       "belief_max_abs_error": float(np.abs(b - b64).max())}
+        out[name] = res
+
+    # c0: 96x128x32 SAD scene, 1 iteration, unit edges
+    g = cases.rng(0)
+    cost, *_ = cases.stereo_cost_from_scene(g, 1, 96, 128, 32, 32)
+    report("stereo_96x128x32_1it", cost, cases.stereo_taps(1, 96, 128, 0.1, 0.5), None,
+           np.ones((1, 4, 96, 128), np.float32), 3, 1, 0, 32)
+    # c1 (crop): 376x310x192, 3 iterations, edges exp(N(0,0.3))
+    g = cases.rng(1)
+    cost, *_ = cases.stereo_cost_from_scene(g, 1, 376, 310, 64, 192)
+    edge = np.exp(g.normal(0, 0.3, size=(1, 4, 376, 310))).astype(np.float32)
+    report("stereo_376x310x192_3it_crop", cost, cases.stereo_taps(1, 376, 310, 0.1, 0.5), None, edge, 3, 3, 0, 192)
+    # c3 (crop): semantic pixel-pairwise, B=2, 256x512, L=19, 2 iterations;
+    # unaries FP16 log-softmax of N(0,2) logits + 32x32 block class bias
+    g = cases.rng(3)
+    B, H, W, L = 2, 256, 512, 19
+    logits = g.normal(0, 2, size=(B, H, W, L)).astype(np.float32)
+    bias = g.normal(0, 2, size=(B, H // 32, W // 32, L)).astype(np.float32)
+    logits += np.repeat(np.repeat(bias, 32, axis=1), 32, axis=2)
+    lsm = logits - logits.max(-1, keepdims=True)
+    lsm = lsm - np.log(np.exp(lsm).sum(-1, keepdims=True))
+    cost = (-lsm.astype(np.float16)).astype(np.float32)
+    j4, _ = cases.semantic_pixel_jump(g, H, W, L)
+    j4 = j4.astype(np.float16).astype(np.float32)  # the FP16 pairwise storage, for every path alike
+    edge = np.ones((B, 4, H, W), np.float32)
+    report("semantic_pixel_2x256x512x19_2it_crop", cost, j4, j4, edge, L, 2, 2, L)
+    return out
 
 
 def cpu_sample_inputs(wc=CPU_CROP_W):
@@ -494,6 +573,8 @@ def main():
     ap.add_argument("--ncu-case", action="store_true", help="small case for ncu captures")
     ap.add_argument("--no-serving", action="store_true", help="skip the served-stream leg")
     ap.add_argument("--serving-only", action="store_true", help="run only the served-stream leg")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the per-config error against the FP64 oracle")
+    ap.add_argument("--accuracy-only", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--serve-load", type=float, default=4.0,
                     help="offered arrival rate as a multiple of the plain per-request capacity")
@@ -502,6 +583,8 @@ def main():
         run_ncu_case(args)
     elif args.serving_only:
         print(json.dumps(run_serving(args)))
+    elif args.accuracy_only:
+        print(json.dumps(run_accuracy()))
     elif args.impl == "reference":
         run_reference(args)
     else:
