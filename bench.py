@@ -339,6 +339,8 @@ def run_ours(args):
         result["serving"] = run_serving(args)
     if rank == 0 and world == 1 and not args.no_accuracy:
         result["accuracy_vs_fp64_oracle"] = run_accuracy()
+    if rank == 0 and world == 1 and not args.no_other:
+        result["other_configs"] = run_other_configs()
     traffic = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic):
         with open(traffic) as fh:
@@ -492,6 +494,73 @@ def run_accuracy():
     return out
 
 
+def run_other_configs():
+    """Device time of the other configurations' ops (inputs resident): the
+    semantic pixel-pairwise pass at 2x512x1024, L=19 (FP32 and FP16 storage,
+    per pass, with the reference adjoint), the flow SAD sub-case 384x512,
+    C=32, window +-32, and the stereo SAD at the full size."""
+    import numpy as np
+    import torch
+    from bpl_gb300 import ops
+    import cases
+    dev = torch.device("cuda", 0)
+
+    def timed(fn, n=3):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(n):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / n
+
+    out = {}
+    g = cases.rng(3)
+    B, Hs, Ws, Ls = 2, 512, 1024, 19
+    cost = torch.from_numpy(cases.random_cost(g, B, Hs, Ws, Ls)).to(dev)
+    j4, _ = cases.semantic_pixel_jump(g, Hs, Ws, Ls)
+    j4 = torch.from_numpy(j4).to(dev)
+    edge = torch.ones((B, 4, Hs, Ws), device=dev)
+    m = torch.zeros((B, 4, Hs, Ws, Ls), device=dev)
+    am = torch.empty((B, 4, Hs, Ws, Ls), dtype=torch.uint8, device=dev)
+    sc = torch.empty((B, 4, Hs, Ws), device=dev)
+    gin = torch.randn((B, 4, Hs, Ws, Ls), device=dev)
+    U = B * Ls * edges(Hs, Ws)
+    fwd = timed(lambda: ops.lbp_forward(ops.LBP_SEM_PIXEL, cost, j4, edge, m, Ls, argmin_dtype=torch.uint8,
+                                        argmin=am, scale=sc))
+    bwd = timed(lambda: ops.lbp_backward(ops.LBP_SEM_PIXEL, None, edge, gin, m, am, sc, copy_grad_messages=False))
+    ch = ops.to_half_padded(cost, Ls)
+    jh = ops.to_half_padded(j4, Ls)
+    Lp = ops.padded_labels(Ls)
+    mh = torch.zeros((B, 4, Hs, Ws, Lp), dtype=torch.float16, device=dev)
+    amh = torch.empty((B, 4, Hs, Ws, Lp), dtype=torch.uint8, device=dev)
+    sch = torch.empty((B, 4, Hs, Ws), device=dev)
+    fwd16 = timed(lambda: ops.lbp_forward_f16(ops.LBP_SEM_PIXEL, ch, jh, edge, mh, Ls, Ls, argmin=amh, scale=sch))
+    out["semantic_pixel_2x512x1024x19"] = {
+        "fp32_forward_pass_ms": fwd, "fp32_backward_pass_ms": bwd, "fp16_forward_pass_ms": fwd16,
+        "updates_per_pass": U, "fp32_forward_updates_per_s": U / (fwd / 1e3),
+        "fp32_forward_GBps": U * (21 + 4 * Ls) / (fwd / 1e3) / 1e9}
+    del cost, j4, m, am, sc, gin, ch, jh, mh, amh, sch
+    f0 = torch.randn((1, 32, 384, 512), device=dev)
+    f1 = torch.randn((1, 32, 384, 512), device=dev)
+    flow = timed(lambda: ops.flow_forward(f0, f1, 64))
+    cu, cv, us, vs = ops.flow_forward(f0, f1, 64)
+    flow_b = timed(lambda: ops.flow_backward(f0, f1, 64, cu, cv, us, vs))
+    out["flow_sad_384x512_C32_w65"] = {"forward_ms": flow, "backward_ms": flow_b,
+                                       "forward_G_absdiff_per_s": 384 * 512 * 65 * 65 * 32 / (flow / 1e3) / 1e9}
+    f0 = torch.randn((1, 64, H, W), device=dev)
+    f1 = torch.randn((1, 64, H, W), device=dev)
+    sad = timed(lambda: ops.sad_forward(f0, f1, 0, L - 1))
+    vol = ops.sad_forward(f0, f1, 0, L - 1)
+    sad_b = timed(lambda: ops.sad_backward(f0, f1, 0, L - 1, vol))
+    out[f"stereo_sad_{H}x{W}_C64_D{L}"] = {"forward_ms": sad, "backward_ms": sad_b,
+                                            "forward_G_absdiff_per_s": H * W * L * 64 / (sad / 1e3) / 1e9,
+                                            "forward_GBps": (4 * 2 * 64 * H * W + 4 * H * W * L) / (sad / 1e3) / 1e9}
+    return out
+
+
 def cpu_sample_inputs(wc=CPU_CROP_W):
     import numpy as np
     import cases
@@ -611,6 +680,8 @@ def main():
     ap.add_argument("--serving-only", action="store_true", help="run only the served-stream leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the per-config error against the FP64 oracle")
     ap.add_argument("--accuracy-only", action="store_true")
+    ap.add_argument("--no-other", action="store_true", help="skip the other configurations' op timings")
+    ap.add_argument("--other-only", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--serve-load", type=float, default=4.0,
                     help="offered arrival rate as a multiple of the plain per-request capacity")
@@ -621,6 +692,8 @@ def main():
         print(json.dumps(run_serving(args)))
     elif args.accuracy_only:
         print(json.dumps(run_accuracy()))
+    elif args.other_only:
+        print(json.dumps(run_other_configs()))
     elif args.impl == "reference":
         run_reference(args)
     else:
