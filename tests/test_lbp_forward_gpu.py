@@ -68,6 +68,14 @@ STEREO_CASES = [
     ("l256_wide", 11, 1, 3, 70, 256, "scalar", 3, 1, None, 1, 1),
     ("l300_k12", 12, 1, 4, 9, 300, "scalar", 3, 1, None, 1, 1),
     ("l19_odd", 13, 2, 7, 8, 19, "scalar", 3, 2, None, 1, 2),
+    # window forms: delta 0 (own label only), 4 (predicated 9-tap window),
+    # 6 (generic scan), 8-tap affinities at delta 3 (beating offsets |jd| <= 2
+    # plus tie-only L3 offsets), and the largest label count
+    ("l48_d0", 16, 1, 6, 11, 48, "scalar", 0, 2, None, 1, 1),
+    ("l40_d4_ties", 17, 1, 7, 12, 40, "scalar", 4, 2, 8, 1, 1),
+    ("l40_d6", 18, 1, 7, 12, 40, "scalar", 6, 2, None, 1, 1),
+    ("l48_taps8_d3_ties", 19, 1, 9, 14, 48, "taps8", 3, 2, 8, 1, 1),
+    ("l1024_max", 20, 1, 3, 5, 1024, "scalar", 3, 1, None, 1, 1),
     # enough scanlines per phase for one warp per scanline (the small cases
     # above split each scanline's labels over several warps)
     ("l64_many_chains", 14, 8, 64, 72, 64, "taps8_off", 3, 1, None, 8, 8),
