@@ -135,15 +135,14 @@ def run_ours(args):
     from bpl_gb300 import ops
     from bpl_gb300.layers.stereo import MessagePassing
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from bpl_gb300 import replicas
+    rank, world, local = replicas.env_ranks()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     if world > 1:
         dist.init_process_group("nccl")
 
-    prob, edge, upstream = synth_inputs(torch, dev, seed=1 + rank)
+    prob, edge, upstream = synth_inputs(torch, dev, seed=replicas.replica_seed(1, rank))
     mp = MessagePassing(dev, ITERS, L, DELTA)
     with torch.no_grad():
         mp._L1.fill_(0.1)
@@ -181,11 +180,7 @@ def run_ours(args):
         torch.cuda.profiler.stop()
     ms = t0.elapsed_time(t1)
     per_op = tm.report()
-    ms_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
+    ms_max = replicas.max_over_ranks(ms, dev)
 
     # ---- e2e through the public API with host buffers --------------------
     # Every step copies its inputs from pinned host memory and its results
@@ -248,11 +243,7 @@ def run_ours(args):
     e2e_run(args.steps)
     e1.record(stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = replicas.max_over_ranks(e0.elapsed_time(e1), dev)
 
     # ---- the same step with FP16 storage of cost and messages -----------------
     fp16 = None
@@ -288,15 +279,15 @@ def run_ours(args):
         f16 = per16.get("lbp_forward_f16", [])
         bw16 = per16.get("lbp_backward_f16", [])
         n16 = args.steps * ITERS
-        fp16 = {"value": updates_per_step() * args.steps * world / (ms16 / 1e3), "unit": UNIT,
+        fp16 = {"value": replicas.whole_job_rate(updates_per_step(), args.steps, world, ms16), "unit": UNIT,
                 "ms_per_step": ms16 / args.steps, "speedup_vs_fp32": ms_max / ms16,
                 "label_agreement_vs_fp32": agree,
                 "lbp_forward_pass_ms": sum(f16) / n16, "lbp_backward_pass_ms": sum(bw16) / n16,
                 "bytes_per_update": {"forward": 11, "backward": 12}}
 
     U = updates_per_step()
-    value = U * args.steps * world / (ms_max / 1e3)
-    e2e_value = U * args.steps * world / (e2e_ms / 1e3)
+    value = replicas.whole_job_rate(U, args.steps, world, ms_max)
+    e2e_value = replicas.whole_job_rate(U, args.steps, world, e2e_ms)
     peak, peak_kind = load_peaks()
     fwd = per_op.get("lbp_forward", [])
     bwd = per_op.get("lbp_backward", [])
