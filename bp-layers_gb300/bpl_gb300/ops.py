@@ -257,10 +257,12 @@ def flow_backward(f0, f1, sws: int, in_grad_u, in_grad_v, u_star, v_star):
     B, C, H, W = f0.shape
     df0 = torch.empty_like(f0)
     df1 = torch.empty_like(f1)
-    st = _timed("flow_backward", lambda: lib().bpl_flow_backward(
+    nws = int(lib().bpl_flow_backward_workspace_size(B, C, H, W))
+    ws = torch.empty((nws + 3) // 4, dtype=torch.float32, device=f0.device)
+    st = _timed("flow_backward", lambda: lib().bpl_flow_backward_ws(
         _ptr(f0), _ptr(f1), _ptr(in_grad_u), _ptr(in_grad_v), _ptr(u_star), _ptr(v_star), _ptr(df0), _ptr(df1),
-        B, C, H, W, int(sws), _stream(f0)))
-    check(st, "bpl_flow_backward")
+        _ptr(ws), nws, B, C, H, W, int(sws), _stream(f0)))
+    check(st, "bpl_flow_backward_ws")
     return df0, df1
 
 

@@ -272,7 +272,9 @@ int bpl_sad_backward(const float* f0, const float* f1, const float* in_grad, flo
  * (B,H,W,K), K = sws+1: cv_u[u] = min over v of the window SAD, u_star[u] =
  * argmin_v + block_v*sws, cv_v[v] = min over u, v_star[v] = argmin_u +
  * block_u*sws (first index on ties; 40 outside the image); bit-identical to
- * the reference.  Windows up to the shared-memory limit (K <= 226).
+ * the reference.  Windows up to K = 256 in one call (the reference's kernel
+ * holds the K x K window in shared memory and stops at K = 128; its Python
+ * layer merges four 108-windows for sws = 216, which equals one call here).
  */
 int bpl_flow_forward(const float* f0, const float* f1, float* cv_u, float* cv_v, float* u_star,
                      float* v_star, int B, int C, int H, int W, int sws, int offset_u, int offset_v,
@@ -282,13 +284,24 @@ int bpl_flow_forward(const float* f0, const float* f1, float* cv_u, float* cv_v,
  * Gradient of the flow SAD.  Replaces cuda::flow_mp_sad_backward
  * (ops/flow_mp_sad/src/flow_mp_sad_kernel.cu:258-290), bound as `backward`
  * (ops/flow_mp_sad/src/flow_mp_sad.cpp:18-30).  df0 is written (bit-identical
- * to the reference), df1 is zero-filled and accumulated with float atomics.
- * Like the reference, offsets are not applied (correct for block 0, zero
- * offsets).
+ * to the reference), df1 is accumulated with float atomics.  Like the
+ * reference, offsets are not applied (correct for block 0, zero offsets).
+ * The scratch (channel-last copies of f1 and df1) is allocated stream-ordered
+ * (cudaMallocAsync) on `stream`; bpl_flow_backward_ws takes it from the
+ * caller instead.
  */
 int bpl_flow_backward(const float* f0, const float* f1, const float* in_grad_u, const float* in_grad_v,
                       const float* u_star, const float* v_star, float* df0, float* df1, int B, int C,
                       int H, int W, int sws, void* stream);
+
+/* Scratch bytes bpl_flow_backward_ws needs: 2*B*C*H*W floats. */
+size_t bpl_flow_backward_workspace_size(int B, int C, int H, int W);
+
+/* bpl_flow_backward with caller-owned scratch (16-byte aligned, at least
+ * bpl_flow_backward_workspace_size bytes; contents on entry are ignored). */
+int bpl_flow_backward_ws(const float* f0, const float* f1, const float* in_grad_u, const float* in_grad_v,
+                         const float* u_star, const float* v_star, float* df0, float* df1, void* workspace,
+                         size_t workspace_bytes, int B, int C, int H, int W, int sws, void* stream);
 
 /*
  * bpl_lbp_backward without device allocation.  No counterpart in the
