@@ -322,7 +322,9 @@ def run_ours(args):
         "kernel_ms": {"lbp_forward_pass": fwd_ms, "lbp_backward_pass": bwd_ms,
                       "forward_GBps_21B": U_pass * FWD_BYTES_PER_UPDATE / (fwd_ms / 1e3) / 1e9 if fwd else None,
                       "backward_GBps_17B": U_pass * BWD_BYTES_PER_UPDATE / (bwd_ms / 1e3) / 1e9 if bwd else None},
-        "gpu_launches": args.steps * (ITERS * 2 + 2 + 2),  # forward passes, batched adjoint, belief epilogue
+        # forward passes (2 phases each), batched adjoint (2 phases), belief
+        # epilogue (forward, backward), the initial messages' gradient
+        "gpu_launches": args.steps * (ITERS * 2 + 2 + 2 + 1),
         "fp16": fp16,
         "clocks": clk.summary(),
     }

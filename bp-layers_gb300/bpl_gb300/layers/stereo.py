@@ -127,6 +127,7 @@ class LBPMinSumFunction(torch.autograd.Function):
         ctx.recompute = recompute
         ctx.delta = int(delta)
         ctx.am_dtype = am_dtype
+        ctx.leaf_messages = messages.is_leaf
         if recompute:
             m_in = messages.detach().clone()
             messages, _, scale = ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta),
@@ -153,6 +154,8 @@ class LBPMinSumFunction(torch.autograd.Function):
         gc, gtaps, ge, gm = ops.lbp_backward(ops.LBP_STEREO, taps, edge, in_grad.contiguous(), messages, argmin,
                                              scale, copy_grad_messages=False, mode=ctx.adjoint)
         g_aff, g_off = unpack_affinity_grad(gtaps)
+        if ctx.leaf_messages and ctx.needs_input_grad[2]:
+            gm = ops.leaf_message_grad(gm)
         return gc, ge, gm, None, g_aff, g_off, None, None
 
 
@@ -172,6 +175,7 @@ class LBPMinSumFunctionF16(torch.autograd.Function):
                                                         argmin_dtype=am_dtype)
         ctx.save_for_backward(taps, edge, messages_h, argmin, scale)
         ctx.L = L
+        ctx.leaf_messages = messages_h.is_leaf
         return messages_h
 
     @staticmethod
@@ -180,7 +184,8 @@ class LBPMinSumFunctionF16(torch.autograd.Function):
         gc, gtaps, ge = ops.lbp_backward_f16(ops.LBP_STEREO, taps, edge, in_grad.contiguous(), messages_h, argmin,
                                              scale, ctx.L)
         g_aff, g_off = unpack_affinity_grad(gtaps)
-        return gc[..., :ctx.L], None, ge, in_grad, None, g_aff, g_off
+        gm = ops.leaf_message_grad(in_grad) if ctx.leaf_messages and ctx.needs_input_grad[3] else in_grad
+        return gc[..., :ctx.L], None, ge, gm, None, g_aff, g_off
 
 
 class LBPMinSumLoop(torch.autograd.Function):
@@ -213,6 +218,7 @@ class LBPMinSumLoop(torch.autograd.Function):
         ctx.save_for_backward(taps, edge, messages, argmins, scales)
         ctx.L = L
         ctx.half = half
+        ctx.leaf_messages = messages.is_leaf
         return messages
 
     @staticmethod
@@ -225,7 +231,8 @@ class LBPMinSumLoop(torch.autograd.Function):
         g_aff, g_off = unpack_affinity_grad(gtaps)
         if ctx.half:
             gc = gc[..., :ctx.L]
-        return gc, None, ge, in_grad, None, g_aff, g_off, None
+        gm = ops.leaf_message_grad(in_grad) if ctx.leaf_messages and ctx.needs_input_grad[3] else in_grad
+        return gc, None, ge, gm, None, g_aff, g_off, None
 
 
 class MessagePassing(nn.Module):

@@ -445,6 +445,32 @@ def beliefs_forward(messages: torch.Tensor, cost: torch.Tensor, temperature: tor
     return out
 
 
+def broadcast_slots(src: torch.Tensor) -> torch.Tensor:
+    """(B, ...) contiguous float or half -> (B, 4, ...) with src in every
+    message slot (a materialised copy of src.unsqueeze(1).expand(...))."""
+    if not src.is_cuda or not src.is_contiguous() or src.dtype not in (torch.float32, torch.float16):
+        raise BplError("broadcast_slots: src must be a contiguous CUDA float or half tensor")
+    B = src.shape[0]
+    dst = torch.empty((B, 4) + tuple(src.shape[1:]), dtype=src.dtype, device=src.device)
+    n = src.numel() // B
+    st = _timed("broadcast_slots", lambda: lib().bpl_broadcast_slots(
+        _ptr(src), _ptr(dst), B, n, src.element_size(), _stream(src)))
+    check(st, "bpl_broadcast_slots")
+    return dst
+
+
+def leaf_message_grad(in_grad: torch.Tensor) -> torch.Tensor:
+    """The message gradient handed to a leaf message tensor: a slot-broadcast
+    in_grad (stride 0 over the slots, as the fused beliefs return it) is
+    written out by one kernel, which autograd then keeps as .grad without a
+    copy of its own; anything else is returned as it is."""
+    if in_grad.dim() == 5 and in_grad.stride(1) == 0 and in_grad.shape[1] == 4:
+        src = in_grad[:, 0]
+        if src.is_contiguous():
+            return broadcast_slots(src)
+    return in_grad
+
+
 def beliefs_backward(messages: torch.Tensor, cost: torch.Tensor, temperature: torch.Tensor, beliefs: torch.Tensor,
                      grad_beliefs: torch.Tensor, want_temperature: bool = True):
     """Gradient of the fused epilogue: (grad_z (B,H,W,L), grad_T (1,) or None)."""

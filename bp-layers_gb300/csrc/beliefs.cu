@@ -175,10 +175,52 @@ int bwd_impl(const T* msgs, const float* cost, const float* Tm, const float* y, 
   return BPL_OK;
 }
 
+// dst (B, 4, n) = src (B, n) repeated over the four message slots, in units
+// of E (16-byte vectors where the rows allow).  grid (x, B)
+template <typename E>
+__global__ void __launch_bounds__(256) slots_broadcast_kernel(const E* __restrict__ src, E* __restrict__ dst,
+                                                              int64_t n) {
+  const int64_t b = blockIdx.y;
+  const E* s = src + b * n;
+  E* d = dst + b * 4 * n;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const E v = __ldg(s + i);
+    d[i] = v;
+    d[n + i] = v;
+    d[2 * n + i] = v;
+    d[3 * n + i] = v;
+  }
+}
+
 }  // namespace
 }  // namespace bpl
 
 using namespace bpl;
+
+extern "C" int bpl_broadcast_slots(const void* src, void* dst, int B, int64_t row_elems, int elem_bytes,
+                                   void* stream) {
+  BPL_REQUIRE(src && dst, "broadcast_slots: null pointer");
+  BPL_REQUIRE(B >= 1 && B <= 65535 && row_elems >= 1, "broadcast_slots: bad shape");
+  BPL_REQUIRE(elem_bytes == 2 || elem_bytes == 4, "broadcast_slots: element size %d not 2 or 4", elem_bytes);
+  const int64_t bytes = row_elems * elem_bytes;
+  const bool vec = bytes % 16 == 0 && reinterpret_cast<uintptr_t>(src) % 16 == 0 &&
+                   reinterpret_cast<uintptr_t>(dst) % 16 == 0;
+  const int64_t n = vec ? bytes / 16 : row_elems;
+  const unsigned gx = static_cast<unsigned>(std::min<int64_t>((n + 255) / 256, 8 * static_cast<int64_t>(sm_count())));
+  const dim3 grid(std::max(1u, gx), B);
+  cudaStream_t st = as_stream(stream);
+  if (vec)
+    slots_broadcast_kernel<uint4><<<grid, 256, 0, st>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), n);
+  else if (elem_bytes == 4)
+    slots_broadcast_kernel<unsigned><<<grid, 256, 0, st>>>(static_cast<const unsigned*>(src),
+                                                           static_cast<unsigned*>(dst), n);
+  else
+    slots_broadcast_kernel<unsigned short><<<grid, 256, 0, st>>>(static_cast<const unsigned short*>(src),
+                                                                 static_cast<unsigned short*>(dst), n);
+  BPL_CUDA_TRY(cudaGetLastError(), "broadcast_slots launch");
+  return BPL_OK;
+}
 
 extern "C" int bpl_beliefs_forward(const void* messages, int messages_half, const float* cost,
                                    const float* temperature, float* beliefs, int B, int H, int W, int L, int Ls,

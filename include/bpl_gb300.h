@@ -219,6 +219,15 @@ int bpl_beliefs_backward(const void* messages, int messages_half, const float* c
                          const float* beliefs, const float* grad_beliefs, float* grad_z, float* grad_temperature,
                          int B, int H, int W, int L, int Ls, void* stream);
 
+/*
+ * dst (B,4,n) = src (B,n) repeated over the four message slots; elements of
+ * elem_bytes (4: float, 2: half).  The message gradient of the reference's
+ * backward (grad_messages = in_grad, ops/lbp_stereo/src/lbp_min_sum_kernel.cu:
+ * 534-536) when in_grad is the beliefs' gradient broadcast over the slots,
+ * written out for a leaf message tensor.
+ */
+int bpl_broadcast_slots(const void* src, void* dst, int B, int64_t row_elems, int elem_bytes, void* stream);
+
 /* Disparity count D of the SAD volume: (int)((max_disp - min_disp + 1) / step)
  * (ops/sad/src/stereo_sad_kernel.cu:122); -1 for a non-positive step. */
 int bpl_sad_volume_depth(int min_disp, int max_disp, float step);

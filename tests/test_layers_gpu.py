@@ -69,6 +69,25 @@ def test_stereo_message_passing_forward_backward():
     np.testing.assert_allclose(got, -gcost, atol=2e-4 * np.abs(gcost).max())
     assert abs(mp._L1.grad.item() - gL1) <= 2e-4 * max(abs(gL1), 1.0)
     assert abs(mp._L2.grad.item() - gL2) <= 2e-4 * max(abs(gL2), 1.0)
+    # the initial messages' gradient: in_grad passed through every pass, i.e.
+    # the beliefs' gradient in each slot, written out as a dense tensor
+    assert m0.grad.is_contiguous() and m0.grad.stride(1) != 0
+    np.testing.assert_allclose(m0.grad.cpu().numpy(), gin, atol=2e-6 * max(np.abs(gin).max(), 1.0))
+
+
+@pytest.mark.parametrize("dtype,shape", [("float32", (2, 5, 7, 48)), ("float16", (1, 3, 5, 24)),
+                                         ("float32", (1, 3, 5, 7)), ("float16", (2, 1, 3, 5))])
+def test_broadcast_slots(dtype, shape):
+    from bpl_gb300 import ops
+    dev = torch.device("cuda:0")
+    src = torch.randn(shape, device=dev).to(getattr(torch, dtype))
+    out = ops.broadcast_slots(src)
+    ref = src.unsqueeze(1).expand(shape[0], 4, *shape[1:])
+    assert torch.equal(out, ref)
+    # leaf_message_grad: a slot-broadcast view is written out, others pass through
+    assert torch.equal(ops.leaf_message_grad(ref), ref) and ops.leaf_message_grad(ref).stride(1) != 0
+    dense = ref.contiguous()
+    assert ops.leaf_message_grad(dense) is dense
 
 
 def test_inference_modes():
