@@ -38,6 +38,7 @@ SIGNATURES = {
     "bpl_flow_backward": [c_void_p] * 8 + [c_int] * 5 + [c_void_p],
     "bpl_flow_backward_workspace_size": [c_int] * 4,
     "bpl_broadcast_slots": [c_void_p] * 2 + [c_int, ctypes.c_int64, c_int, c_void_p],
+    "bpl_upsample_add_beliefs": [c_void_p] * 2 + [c_int] * 4 + [ctypes.c_float, c_void_p],
     "bpl_flow_backward_ws": [c_void_p] * 9 + [ctypes.c_size_t] + [c_int] * 5 + [c_void_p],
     "bpl_lbp_backward_noalloc": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 4 + [c_int] * 7 + [c_void_p],
 }

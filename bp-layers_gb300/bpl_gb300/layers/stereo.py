@@ -361,6 +361,92 @@ class Inference(nn.Module):
         return torch.sum(bw * win, dim=-1, keepdim=True)
 
 
+class BP(nn.Module):
+    """ops/lbp_stereo/bp_op_cuda.py:80-127: MessagePassing plus Inference
+    for a disparity volume (N,H,W,K) or a flow volume (N,2,H,W,K).
+
+    The flow path is the reference's: u, then v, each from zero messages
+    created with requires_grad, except that the v pass is handed the u
+    pass's messages (bp_op_cuda.py:110 passes messages_u), which the u pass
+    has updated in place, so v starts from u's final messages and both
+    entries of the returned messages are that tensor after v.  With
+    joint_flow=True the u and v volumes instead run as one batch of 2N items
+    from zero messages each: one launch per kernel for both, twice the
+    scanlines for the latency-bound sweeps; the results are those of two
+    independent calls.  Checkpoint loading (SubNetwork) is not part of this
+    module."""
+
+    def __init__(self, device, args=None, max_iter=1, num_labels=None, delta=1, mode_inference="expectation",
+                 mode_message_passing="min-sum", layer_idx=0, level=0, joint_flow=False, **mp_options):
+        super().__init__()
+        if mode_inference not in ("wta", "expectation", "norm", "raw", "sub-exp") or mode_message_passing != "min-sum":
+            raise ValueError("Unknown inference/message passing mode " + mode_inference + " " + mode_message_passing)
+        self.device = device
+        self.max_iter = max_iter
+        self.layer_idx = layer_idx
+        self.level = level
+        self.delta = delta
+        self.joint_flow = joint_flow
+        self.message_passing = MessagePassing(device, max_iter, num_labels, delta, mode_message_passing,
+                                              **mp_options)
+        self.inference = Inference(device, mode_inference, mode_passing=mode_message_passing)
+
+    def _zeros(self, N, H, W, K):
+        return torch.zeros((N, 4, H, W, K), requires_grad=True, device=self.device, dtype=torch.float)
+
+    def forward(self, prob_vol, edge_weights, affinities=None, offsets=None):
+        if prob_vol.dim() == 5:
+            N, _, H, W, K = prob_vol.shape
+            if self.joint_flow:
+                pv = torch.cat((prob_vol[:, 0], prob_vol[:, 1]), dim=0).contiguous()
+                twice = (lambda t: None if t is None else torch.cat((t, t), dim=0).contiguous())
+                beliefs, messages = self.message_passing.forward(pv, twice(edge_weights), twice(affinities),
+                                                                 twice(offsets), self._zeros(2 * N, H, W, K))
+                result = self.inference.forward(beliefs)
+                flow = torch.cat((result[:N], result[N:]), dim=-1).permute(0, 3, 1, 2)
+                beliefs = torch.stack((beliefs[:N], beliefs[N:]), dim=1)
+                messages = torch.stack((messages[:N], messages[N:]), dim=1)
+                return flow, beliefs, messages
+            messages_u = self._zeros(N, H, W, K)
+            beliefs_u, messages_u = self.message_passing.forward(prob_vol[:, 0].contiguous(), edge_weights,
+                                                                 affinities, offsets, messages_u)
+            result_u = self.inference.forward(beliefs_u)
+            beliefs_v, messages_v = self.message_passing.forward(prob_vol[:, 1].contiguous(), edge_weights,
+                                                                 affinities, offsets, messages_u)
+            result_v = self.inference.forward(beliefs_v)
+            flow = torch.cat((result_u, result_v), dim=-1).permute(0, 3, 1, 2)
+            beliefs = torch.cat((beliefs_u.unsqueeze(1), beliefs_v.unsqueeze(1)), dim=1)
+            messages = torch.cat((messages_u.unsqueeze(1), messages_v.unsqueeze(1)), dim=1)
+            return flow, beliefs, messages
+        N, H, W, K = prob_vol.shape
+        messages = self._zeros(N, H, W, K)
+        beliefs, messages = self.message_passing.forward(prob_vol.contiguous(), edge_weights, affinities, offsets,
+                                                         messages)
+        result = self.inference.forward(beliefs)
+        return result.permute(0, 3, 1, 2), beliefs, messages
+
+    adjust_input_weights = staticmethod(lambda weights, idx: adjust_input_weights(weights, idx))
+    adjust_input_affinities = staticmethod(lambda affinities: adjust_input_affinities(affinities))
+    adjust_input_offsets = staticmethod(lambda offsets: adjust_input_offsets(offsets))
+
+    def project_jumpcosts(self):
+        self.message_passing.projectL1L2()
+
+
+def coarse_to_fine(beliefs_in, pv_lvl):
+    """The step between two BP levels of the stereo network (stereo.py:
+    104-113): with the coarse beliefs requiring a gradient the reference only
+    normalises the finer probability volume over its labels (the upsampled
+    beliefs are dropped); otherwise it adds the beliefs, upsampled by 2
+    trilinearly along rows, columns and labels and halved, in place, which
+    is one kernel here.  Returns the volume for the finer level."""
+    if beliefs_in is None:
+        return pv_lvl
+    if beliefs_in.requires_grad:
+        return pv_lvl / pv_lvl.sum(dim=-1, keepdim=True)
+    return ops.upsample_add_beliefs(beliefs_in.contiguous(), pv_lvl, 0.5)
+
+
 def adjust_input_weights(weights, idx):
     """bp_op_cuda.py:130-154: (N,2,H,W) x/y weights -> (N,4,H,W) per direction."""
     if weights is None:

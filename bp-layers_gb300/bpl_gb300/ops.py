@@ -459,6 +459,20 @@ def broadcast_slots(src: torch.Tensor) -> torch.Tensor:
     return dst
 
 
+def upsample_add_beliefs(beliefs: torch.Tensor, pv: torch.Tensor, weight: float = 0.5) -> torch.Tensor:
+    """pv (N,2h,2w,2d) += weight * trilinear x2 upsampling of beliefs
+    (N,h,w,d), in place (stereo.py:104-113 with weight 0.5); returns pv."""
+    _check_input("beliefs", beliefs, dim=4)
+    _check_input("pv", pv, dim=4)
+    N, h, w, d = beliefs.shape
+    if tuple(pv.shape) != (N, 2 * h, 2 * w, 2 * d):
+        raise BplError(f"pv must be {(N, 2 * h, 2 * w, 2 * d)}, got {tuple(pv.shape)}")
+    st = _timed("upsample_add_beliefs", lambda: lib().bpl_upsample_add_beliefs(
+        _ptr(beliefs), _ptr(pv), N, h, w, d, float(weight), _stream(pv)))
+    check(st, "bpl_upsample_add_beliefs")
+    return pv
+
+
 def leaf_message_grad(in_grad: torch.Tensor) -> torch.Tensor:
     """The message gradient handed to a leaf message tensor: a slot-broadcast
     in_grad (stride 0 over the slots, as the fused beliefs return it) is

@@ -228,6 +228,15 @@ int bpl_beliefs_backward(const void* messages, int messages_half, const float* c
  */
 int bpl_broadcast_slots(const void* src, void* dst, int B, int64_t row_elems, int elem_bytes, void* stream);
 
+/*
+ * Coarse-to-fine glue (stereo.py:104-113): pv (N,2h,2w,2d) += weight *
+ * trilinear x2 upsampling of beliefs (N,h,w,d) over rows, columns and labels
+ * (F.interpolate(scale_factor=2.0, mode='trilinear'), align_corners False;
+ * the reference adds it halved: weight 0.5).  In place on pv, one pass.
+ */
+int bpl_upsample_add_beliefs(const float* beliefs, float* pv, int N, int h, int w, int d, float weight,
+                             void* stream);
+
 /* Disparity count D of the SAD volume: (int)((max_disp - min_disp + 1) / step)
  * (ops/sad/src/stereo_sad_kernel.cu:122); -1 for a non-positive step. */
 int bpl_sad_volume_depth(int min_disp, int max_disp, float step);
