@@ -491,7 +491,9 @@ def run_other_configs():
     """Device time of the other configurations' ops (inputs resident): the
     semantic pixel-pairwise pass at 2x512x1024, L=19 (FP32 and FP16 storage,
     per pass, with the reference adjoint), the flow SAD sub-case 384x512,
-    C=32, window +-32, and the stereo SAD at the full size."""
+    C=32, window +-32 (and +-108 in one call), the flow BP in the reference's
+    order and as one batch, the coarse-to-fine glue, and the stereo SAD at
+    the full size."""
     import numpy as np
     import torch
     from bpl_gb300 import ops
@@ -543,6 +545,32 @@ def run_other_configs():
     flow_b = timed(lambda: ops.flow_backward(f0, f1, 64, cu, cv, us, vs))
     out["flow_sad_384x512_C32_w65"] = {"forward_ms": flow, "backward_ms": flow_b,
                                        "forward_G_absdiff_per_s": 384 * 512 * 65 * 65 * 32 / (flow / 1e3) / 1e9}
+    del cu, cv, us, vs
+    flow2 = timed(lambda: ops.flow_forward(f0, f1, 216), n=1)
+    cu, cv, us, vs = ops.flow_forward(f0, f1, 216)
+    flow2_b = timed(lambda: ops.flow_backward(f0, f1, 216, cu, cv, us, vs), n=1)
+    out["flow_sad_384x512_C32_w217_one_call"] = {"forward_ms": flow2, "backward_ms": flow2_b}
+    del cu, cv, us, vs, f0, f1
+    # flow BP (bp_op_cuda.py:100-117) on a 384x512 two-component volume,
+    # 65 labels, 3 iterations, inference: the reference's u-then-v order
+    # against u and v as one batch
+    from bpl_gb300.layers.stereo import BP, coarse_to_fine
+    pvf = torch.softmax(torch.randn((1, 2, 384, 512, 65), device=dev), dim=-1)
+    ew = torch.ones((1, 4, 384, 512), device=dev)
+    with torch.no_grad():
+        seq = BP(dev, None, 3, 65, 3, mode_inference="wta")
+        joint = BP(dev, None, 3, 65, 3, mode_inference="wta", joint_flow=True)
+        t_seq = timed(lambda: seq(pvf, ew))
+        t_joint = timed(lambda: joint(pvf, ew))
+    out["flow_bp_384x512x65_3it"] = {"reference_order_ms": t_seq, "joint_ms": t_joint}
+    del pvf, ew
+    # coarse-to-fine glue (stereo.py:104-113) into the full-size volume
+    bc = torch.softmax(torch.randn((1, H // 2, W // 2, L // 2), device=dev), dim=-1)
+    pvl = torch.softmax(torch.randn((1, H, W, L), device=dev), dim=-1)
+    glue = timed(lambda: coarse_to_fine(bc, pvl))
+    out[f"coarse_to_fine_{H // 2}x{W // 2}x{L // 2}_to_{H}x{W}x{L}"] = {
+        "ms": glue, "GBps": (8 * H * W * L + bc.numel() * 4) / (glue / 1e3) / 1e9}
+    del bc, pvl
     f0 = torch.randn((1, 64, H, W), device=dev)
     f1 = torch.randn((1, 64, H, W), device=dev)
     sad = timed(lambda: ops.sad_forward(f0, f1, 0, L - 1))
@@ -625,8 +653,9 @@ def run_ncu_case(args):
     second run of each): LBP forward and reference adjoint at 256x512x192
     (cost 100 MB, messages 400 MB: larger than L2, well under the capture
     size limit), the exact adjoint's message-gradient assembly, the belief
-    epilogue, SAD at 384x512 C=64 D=192 and the flow SAD at 384x512 C=32,
-    window +-32."""
+    epilogue, SAD at 384x512 C=64 D=192, the flow SAD at 384x512 C=32,
+    window +-32, the coarse-to-fine glue into 256x512x192 and the slot
+    broadcast of a 256x512x192 volume."""
     import torch
     from bpl_gb300 import ops
     import cases
@@ -642,6 +671,8 @@ def run_ncu_case(args):
     f1 = torch.randn((1, 64, 384, 512), device=dev)
     g0 = torch.randn((1, 32, 384, 512), device=dev)
     g1 = torch.randn((1, 32, 384, 512), device=dev)
+    bc = torch.rand((1, h // 2, w // 2, L // 2), device=dev)
+    pvl = torch.rand((1, h, w, L), device=dev)
     for it in range(2):
         if it == 1:
             torch.cuda.synchronize()
@@ -655,6 +686,8 @@ def run_ncu_case(args):
         ops.sad_backward(f0, f1, 0, L - 1, vol)
         cu, cv, us, vs = ops.flow_forward(g0, g1, 64)
         ops.flow_backward(g0, g1, 64, cu, cv, us, vs)
+        ops.upsample_add_beliefs(bc, pvl, 0.5)
+        ops.broadcast_slots(cost)
         torch.cuda.synchronize()
     torch.cuda.profiler.stop()
     print(json.dumps({"ncu_case": f"{h}x{w}x{L}", "updates_per_pass": L * edges(h, w)}))

@@ -17,11 +17,14 @@
 // channel chunks are double-buffered (cp.async of chunk i+1 while chunk i is
 // summed), because a 512-thread block leaves one block per SM and a
 // synchronous load per chunk stalled the whole SM.
-// Backward: one thread per (channel, pixel) walks the disparities in the
-// reference order (additions of +-g in the same sequence: bit-identical); the
-// upstream gradient is staged per chunk of disparities in shared memory,
-// shared by the block's 16 channels (read directly, a warp's lanes were D
-// floats apart: one sector per lane and load).
+// Backward: lanes are channels and each thread owns 4 pixels; both sums walk
+// the disparities in the reference order (additions of +-g in the same
+// sequence: bit-identical).  Per chunk of 32 disparities the block stages
+// (cp.async, double-buffered) its channels' f1 segment x - d, f0 segment
+// x + d and the two gradient tables g[x, d] and g[x + d, d], which the warp
+// reads as broadcasts; the thread slides a register window over its feature
+// rows, so a term is a subtraction, a sign-bit operation, the |diff| test
+// and a predicated add (ALU-pipe bound).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -201,69 +204,138 @@ struct SadBwdArgs {
   int channel_limit;
 };
 
-constexpr int kBX = 32;   // pixels per block (backward)
-constexpr int kBC = 16;   // channels per block
-constexpr int kBD = 32;   // disparities per staged chunk
-constexpr int kBS = kBD + 1;  // padded row stride of the staged chunks
+constexpr int kBX = 32;            // pixels per block (backward)
+constexpr int kBPX = 4;            // pixels per thread
+constexpr int kBCH = 32;           // channels per block: lane = channel
+constexpr int kBDC = 32;           // disparities per staged chunk
+constexpr int kBFS = kBX + kBDC - 1;  // staged feature row (odd: lanes' rows fall in distinct banks)
 
-// grid (ceil(W/kBX), H, B*ceil(C/kBC)); block kBX x kBC threads, one per
-// (channel, pixel), each summing over the disparities in the reference's
-// order.  The upstream gradient is staged per chunk of kBD disparities,
-// shared by the block's channels: gA[px][dd] = g[y, x0+px, d0+dd] (df0) and
-// the diagonal band gD[s][dd] = g[y, x0+d0+s, d0+dd] (df1 reads s = px+dd),
-// rows padded to kBS floats so a warp's reads fall in distinct banks.
-__global__ void __launch_bounds__(kBX * kBC) sad_backward_kernel(SadBwdArgs a) {
-  __shared__ float gA[kBX * kBS];
-  __shared__ float gD[(kBX + kBD - 1) * kBS];
-  const int ncb = (a.C + kBC - 1) / kBC;
+// One term of the reference's sums: acc += (diff/|diff|) * g when |diff| >
+// 1e-15 (df0), acc -= ... (df1).  diff/|diff| is exactly +-1, so the update
+// is g with the sign of diff (flipped for df1): one sign-bit operation; a
+// NaN diff never passes the test, as in the reference.
+template <bool NEG>
+__device__ __forceinline__ void sad_term(float& acc, float diff, float g) {
+  const unsigned sb = (NEG ? ~__float_as_uint(diff) : __float_as_uint(diff)) & 0x80000000u;
+  const float t = __uint_as_float(__float_as_uint(g) ^ sb);
+  if (fabsf(diff) > 1e-15f) acc = __fadd_rn(acc, t);
+}
+
+// grid (ceil(W/32), H, B*ceil(C/32)); block 256 = 8 warps.  Warp w owns
+// pixels x0 + 4w .. +3, lane the channel; both sums run over d ascending
+// (the reference's order), chunk by chunk of 32 disparities staged in
+// shared memory: the f1 row segment x - d and the f0 row segment x + d of
+// the block's channels (NaN outside the image, which the |diff| test drops
+// like the reference's bounds checks), g[y, x, d] and the diagonal
+// g[y, x + d, d] (zero past max_disp: a zero update leaves the sum as it
+// is, which is never -0).  Each thread slides a 4-value window over the
+// staged rows, so a disparity costs it one new value per row and one
+// broadcast 16-byte load per gradient table.
+__global__ void __launch_bounds__(256, 1) sad_backward_kernel(SadBwdArgs a) {
+  // two buffers: chunk ci + 1 lands (cp.async) while chunk ci is summed
+  __shared__ float f1s[2][kBCH * kBFS];   // f1[c, x0 - d0 - 31 + k]
+  __shared__ float f0s[2][kBCH * kBFS];   // f0[c, x0 + d0 + k]
+  __shared__ __align__(16) float gA[2][kBDC * kBX];  // g[y, x0 + x, d0 + dd]
+  __shared__ __align__(16) float gD[2][kBDC * kBX];  // g[y, x0 + x + d0 + dd, d0 + dd]
+  const int ncb = (a.C + kBCH - 1) / kBCH;
   const int n = blockIdx.z / ncb;
-  const int c = (blockIdx.z % ncb) * kBC + threadIdx.y;
+  const int c0 = (blockIdx.z % ncb) * kBCH;
   const int y = blockIdx.y;
   const int x0 = blockIdx.x * kBX;
-  const int x = x0 + threadIdx.x;
-  const int tid = threadIdx.y * kBX + threadIdx.x;
-  const bool act = x < a.W && c < a.C && c < a.channel_limit;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int c = c0 + lane;
   const int64_t HW = static_cast<int64_t>(a.H) * a.W;
   const float* grow = a.g + ((static_cast<int64_t>(n) * a.H + y) * a.W) * a.D;
-  const int cc = act ? c : 0;
-  const float* r0 = a.f0 + (static_cast<int64_t>(n) * a.C + cc) * HW + static_cast<int64_t>(y) * a.W;
-  const float* r1 = a.f1 + (static_cast<int64_t>(n) * a.C + cc) * HW + static_cast<int64_t>(y) * a.W;
-  const float a0 = act ? r0[x] : 0.0f, b0 = act ? r1[x] : 0.0f;
-  float g0 = 0.0f, g1 = 0.0f;
-  for (int d0 = a.min_disp; d0 <= a.max_disp; d0 += kBD) {
-    const int i0 = d0 - a.min_disp;  // volume index of d0
-    const int nd = min(kBD, a.max_disp - d0 + 1);
-    __syncthreads();
-    for (int e = tid; e < kBX * kBD; e += kBX * kBC) {
-      const int px = e / kBD, dd = e % kBD, xx = x0 + px;
-      gA[px * kBS + dd] = (xx < a.W && dd < nd) ? __ldg(grow + static_cast<int64_t>(xx) * a.D + i0 + dd) : 0.0f;
+  const float* f0b = a.f0 + (static_cast<int64_t>(n) * a.C + c0) * HW + static_cast<int64_t>(y) * a.W;
+  const float* f1b = a.f1 + (static_cast<int64_t>(n) * a.C + c0) * HW + static_cast<int64_t>(y) * a.W;
+  const float qnan = __int_as_float(0x7fffffff);
+  // the thread's own pixels: f0[c, x] (df0) and f1[c, x] (df1)
+  float a0[kBPX], b0[kBPX], acc0[kBPX], acc1[kBPX];
+#pragma unroll
+  for (int i = 0; i < kBPX; ++i) {
+    const int x = x0 + 4 * w + i;
+    const bool ok = c < a.C && x < a.W;
+    a0[i] = ok ? __ldg(f0b + lane * HW + x) : 0.0f;
+    b0[i] = ok ? __ldg(f1b + lane * HW + x) : 0.0f;
+    acc0[i] = 0.0f;
+    acc1[i] = 0.0f;
+  }
+  // stage chunk ci into buffer ci & 1: cp.async for what lies inside the
+  // image and the disparity range, plain stores of the fill values
+  const int nchunk = (a.max_disp - a.min_disp) / kBDC + 1;
+  auto stage = [&](int ci) {
+    const int b = ci & 1;
+    const int d0 = a.min_disp + ci * kBDC;
+    const int i0 = d0 - a.min_disp;
+    const int nd = min(kBDC, a.max_disp - d0 + 1);
+    for (int e = tid; e < kBCH * kBFS; e += 256) {
+      const int cc = e / kBFS, k = e - cc * kBFS;
+      const bool cok = c0 + cc < a.C;
+      const int xa = x0 - d0 - (kBDC - 1) + k, xb = x0 + d0 + k;
+      if (cok && xa >= 0 && xa < a.W) cp_async4(&f1s[b][e], f1b + cc * HW + xa);
+      else f1s[b][e] = qnan;
+      if (cok && xb >= 0 && xb < a.W) cp_async4(&f0s[b][e], f0b + cc * HW + xb);
+      else f0s[b][e] = qnan;
     }
-    for (int e = tid; e < (kBX + kBD - 1) * kBD; e += kBX * kBC) {
-      const int sr = e / kBD, dd = e % kBD, xx = x0 + d0 + sr;
-      gD[sr * kBS + dd] =
-          (xx >= 0 && xx < a.W && dd < nd) ? __ldg(grow + static_cast<int64_t>(xx) * a.D + i0 + dd) : 0.0f;
+    for (int e = tid; e < kBDC * kBX; e += 256) {
+      const int dd = e / kBX, x = e - dd * kBX;
+      const int xa = x0 + x, xd = x0 + x + d0 + dd;
+      if (dd < nd && xa < a.W) cp_async4(&gA[b][e], grow + static_cast<int64_t>(xa) * a.D + i0 + dd);
+      else gA[b][e] = 0.0f;
+      if (dd < nd && xd >= 0 && xd < a.W) cp_async4(&gD[b][e], grow + static_cast<int64_t>(xd) * a.D + i0 + dd);
+      else gD[b][e] = 0.0f;
+    }
+    cp_async_commit();
+  };
+  stage(0);
+  for (int ci = 0; ci < nchunk; ++ci) {
+    const int b = ci & 1;
+    if (ci + 1 < nchunk) {
+      stage(ci + 1);  // buffer (ci + 1) & 1 was last read by chunk ci - 1, before its closing barrier
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
     __syncthreads();
-    if (act) {
-      for (int dd = 0; dd < nd; ++dd) {
-        const int d = d0 + dd;
-        if (x - d >= 0 && x - d < a.W) {
-          const float diff = __fsub_rn(a0, __ldg(r1 + x - d));
-          const float gv = gA[threadIdx.x * kBS + dd];
-          if (fabsf(diff) > 1e-15f) g0 = (diff > 0.0f) ? __fadd_rn(g0, gv) : __fsub_rn(g0, gv);
-        }
-        if (x + d >= 0 && x + d < a.W) {
-          const float diff1 = __fsub_rn(__ldg(r0 + x + d), b0);
-          // g[y, x+d, d]: band row (x - x0) + dd (requires x + d = x0 + d0 + row)
-          const float gv = gD[(threadIdx.x + dd) * kBS + dd];
-          if (fabsf(diff1) > 1e-15f) g1 = (diff1 > 0.0f) ? __fsub_rn(g1, gv) : __fadd_rn(g1, gv);
-        }
+    const float* F1 = f1s[b] + lane * kBFS + 4 * w + (kBDC - 1);  // F1[i - dd] = f1[c, x0 + 4w + i - (d0 + dd)]
+    const float* F0 = f0s[b] + lane * kBFS + 4 * w;               // F0[i + dd] = f0[c, x0 + 4w + i + (d0 + dd)]
+    float v1[kBPX], v0[kBPX];
+#pragma unroll
+    for (int i = 0; i < kBPX; ++i) {
+      v1[i] = F1[i];
+      v0[i] = F0[i];
+    }
+#pragma unroll
+    for (int dd = 0; dd < kBDC; ++dd) {
+      if (dd > 0) {
+#pragma unroll
+        for (int i = kBPX - 1; i > 0; --i) v1[i] = v1[i - 1];
+        v1[0] = F1[-dd];
+#pragma unroll
+        for (int i = 0; i < kBPX - 1; ++i) v0[i] = v0[i + 1];
+        v0[kBPX - 1] = F0[kBPX - 1 + dd];
+      }
+      const float4 ga = *reinterpret_cast<const float4*>(gA[b] + dd * kBX + 4 * w);
+      const float4 gd = *reinterpret_cast<const float4*>(gD[b] + dd * kBX + 4 * w);
+      const float gav[4] = {ga.x, ga.y, ga.z, ga.w};
+      const float gdv[4] = {gd.x, gd.y, gd.z, gd.w};
+#pragma unroll
+      for (int i = 0; i < kBPX; ++i) {
+        sad_term<false>(acc0[i], __fsub_rn(a0[i], v1[i]), gav[i]);
+        sad_term<true>(acc1[i], __fsub_rn(v0[i], b0[i]), gdv[i]);
       }
     }
+    __syncthreads();  // buffer b is restaged by chunk ci + 2
   }
-  if (!act) return;
-  a.df0[(static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W + x] = g0;
-  a.df1[(static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W + x] = g1;
+  if (c >= a.C || c >= a.channel_limit) return;
+#pragma unroll
+  for (int i = 0; i < kBPX; ++i) {
+    const int x = x0 + 4 * w + i;
+    if (x >= a.W) continue;
+    const int64_t o = (static_cast<int64_t>(n) * a.C + c) * HW + static_cast<int64_t>(y) * a.W + x;
+    a.df0[o] = acc0[i];
+    a.df1[o] = acc1[i];
+  }
 }
 
 }  // namespace
@@ -324,8 +396,9 @@ extern "C" int bpl_sad_backward(const float* f0, const float* f1, const float* i
   if (reference_channel_limit) a.channel_limit = std::min(C, 4 * ((D + 3) / 4));
   BPL_CUDA_TRY(cudaMemsetAsync(df0, 0, sizeof(float) * B * C * H * W, as_stream(stream)), "sad_backward: memset");
   BPL_CUDA_TRY(cudaMemsetAsync(df1, 0, sizeof(float) * B * C * H * W, as_stream(stream)), "sad_backward: memset");
-  dim3 grid((W + kBX - 1) / kBX, H, B * ((C + kBC - 1) / kBC));
-  sad_backward_kernel<<<grid, dim3(kBX, kBC), 0, as_stream(stream)>>>(a);
+  BPL_REQUIRE(static_cast<int64_t>(B) * ((C + kBCH - 1) / kBCH) <= 65535 && H <= 65535, "sad_backward: grid too large");
+  dim3 grid((W + kBX - 1) / kBX, H, B * ((C + kBCH - 1) / kBCH));
+  sad_backward_kernel<<<grid, 256, 0, as_stream(stream)>>>(a);
   BPL_CUDA_TRY(cudaGetLastError(), "sad_backward launch");
   return BPL_OK;
 }

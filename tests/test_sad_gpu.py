@@ -19,6 +19,8 @@ CASES = [
     ("c5_d7_odd", 6, 1, 5, 7, 33, 2, 8, 1.0, 4),
     ("step_half", 7, 1, 6, 5, 40, 0, 9, 0.5, None),
     ("c16_d256", 8, 1, 16, 2, 520, 0, 255, 1.0, None),
+    ("c40_d20_min1", 9, 1, 40, 4, 50, 1, 20, 1.0, 2),
+    ("c33_dneg_wide", 10, 1, 33, 3, 37, -40, 45, 1.0, None),
 ]
 
 
