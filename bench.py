@@ -537,7 +537,31 @@ def run_other_configs():
         "fp32_forward_pass_ms": fwd, "fp32_backward_pass_ms": bwd, "fp16_forward_pass_ms": fwd16,
         "updates_per_pass": U, "fp32_forward_updates_per_s": U / (fwd / 1e3),
         "fp32_forward_GBps": U * (21 + 4 * Ls) / (fwd / 1e3) / 1e9}
-    del cost, j4, m, am, sc, gin, ch, jh, mh, amh, sch
+    # one pass of the layer (message_passing_op_pw_pixel.py:27-51): the
+    # reference's per-pass packing into (4,H,W,L,L) and the fold of the jump
+    # gradient, against the two planes read and accumulated by the kernels
+    jp = torch.from_numpy(g.uniform(0.0, 1.5, size=(2, Hs, Ws, Ls, Ls)).astype(np.float32)).to(dev)
+
+    def packed_pass():
+        js = torch.zeros((4, Hs, Ws, Ls, Ls), device=dev)
+        js[0] = jp[0]
+        js[1, :, 1:] = jp[0, :, :-1].permute(0, 1, 3, 2)
+        js[2] = jp[1]
+        js[3, 1:] = jp[1, :-1].permute(0, 1, 3, 2)
+        ops.lbp_forward(ops.LBP_SEM_PIXEL, cost, js.contiguous(), edge, m, Ls, argmin_dtype=torch.uint8, argmin=am,
+                        scale=sc)
+        _, gj, _, _ = ops.lbp_backward(ops.LBP_SEM_PIXEL, None, edge, gin, m, am, sc, copy_grad_messages=False)
+        gj[0, :, :-1] += gj[1, :, 1:].permute(0, 1, 3, 2)
+        gj[1] = gj[2]
+        gj[1, :-1] += gj[3, 1:].permute(0, 1, 3, 2)
+
+    def planes_pass():
+        ops.lbp_forward(ops.LBP_SEM_PIXEL_LAYER, cost, jp, edge, m, Ls, argmin_dtype=torch.uint8, argmin=am, scale=sc)
+        ops.lbp_backward(ops.LBP_SEM_PIXEL_LAYER, None, edge, gin, m, am, sc, copy_grad_messages=False)
+
+    out["semantic_pixel_2x512x1024x19"]["layer_pass_fwd_bwd_ms"] = {"materialised_packing": timed(packed_pass),
+                                                                      "two_planes_in_kernels": timed(planes_pass)}
+    del cost, j4, m, am, sc, gin, ch, jh, mh, amh, sch, jp
     f0 = torch.randn((1, 32, 384, 512), device=dev)
     f1 = torch.randn((1, 32, 384, 512), device=dev)
     flow = timed(lambda: ops.flow_forward(f0, f1, 64))

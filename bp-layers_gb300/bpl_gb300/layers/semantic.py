@@ -91,36 +91,29 @@ class MessagePassingGlobal(nn.Module):
 
 class LBPMinSumFunctionPixel(torch.autograd.Function):
     """forward(cost, L1, L2, edge, messages, delta, jump) with jump
-    (2,H,W,L,L): shifted/transposed to (4,H,W,L,L)
-    (message_passing_op_pw_pixel.py:147-158); the gradient is folded back
-    the same way (:175-180)."""
+    (2,H,W,L,L), the LR and UD pairwise planes.  The reference layer builds
+    a shifted and transposed (4,H,W,L,L) copy on every pass
+    (message_passing_op_pw_pixel.py:27-38) and folds the (4,H,W,L,L) jump
+    gradient back to two planes (:47-51); here the kernels read the two
+    planes with that shift and transpose and accumulate the gradient in the
+    two-plane layout (variant LBP_SEM_PIXEL_LAYER), so neither copy exists."""
 
     @staticmethod
     def forward(ctx, cost, L1, L2, edge, messages, delta, jump):
-        js = torch.zeros((jump.shape[0] + 2,) + tuple(jump.shape[1:]), dtype=torch.float32, device=cost.device)
-        js[0] = jump[0]
-        js[1, :, 1:] = jump[0, :, :-1].permute((0, 1, 3, 2))
-        js[2] = jump[1]
-        js[3, 1:] = jump[1, :-1].permute((0, 1, 3, 2))
-        js = js.contiguous()
         L = cost.shape[-1]
-        messages, argmin, scale = ops.lbp_forward(ops.LBP_SEM_PIXEL, cost, js, edge, messages, int(delta),
-                                                  argmin_dtype=_argmin_dtype(L))
+        messages, argmin, scale = ops.lbp_forward(ops.LBP_SEM_PIXEL_LAYER, cost, jump.contiguous(), edge, messages,
+                                                  int(delta), argmin_dtype=_argmin_dtype(L))
         ctx.save_for_backward(edge, messages, argmin, scale)
         return messages
 
     @staticmethod
     def backward(ctx, in_grad):
         edge, messages, argmin, scale = ctx.saved_tensors
-        gc, gj, _, gm = ops.lbp_backward(ops.LBP_SEM_PIXEL, None, edge, in_grad.contiguous(), messages, argmin, scale,
-                                         copy_grad_messages=False)
-        gj[0, :, :-1] += gj[1, :, 1:].permute((0, 1, 3, 2))
-        gj[1] = 0
-        gj[1] += gj[2]
-        gj[1, :-1] += gj[3, 1:].permute((0, 1, 3, 2))
+        gc, gj, _, gm = ops.lbp_backward(ops.LBP_SEM_PIXEL_LAYER, None, edge, in_grad.contiguous(), messages, argmin,
+                                         scale, copy_grad_messages=False)
         # no edge gradient in the reference's pixel variant
         ge = torch.zeros_like(edge)
-        return gc, None, None, ge, gm, None, gj[:2]
+        return gc, None, None, ge, gm, None, gj
 
 
 class MessagePassingPixel(nn.Module):

@@ -13,6 +13,18 @@ import torch
 from ._lib import BplError, check, lib
 
 LBP_STEREO, LBP_SEM_GLOBAL, LBP_SEM_PIXEL = 0, 1, 2
+# the pixel variant fed the layer's (2,H,W,L,L) LR / UD pairwise planes (the
+# kernels apply the shift and transpose of message_passing_op_pw_pixel.py:
+# 27-38; the jump gradient comes back in the same two-plane layout)
+LBP_SEM_PIXEL_LAYER = 3
+
+
+def _pixel(variant: int) -> bool:
+    return variant in (LBP_SEM_PIXEL, LBP_SEM_PIXEL_LAYER)
+
+
+def _pixel_planes(variant: int) -> int:
+    return 2 if variant == LBP_SEM_PIXEL_LAYER else 4
 ARGMIN_NONE, ARGMIN_F32, ARGMIN_U8, ARGMIN_U16 = 0, 1, 2, 3
 
 _ARGMIN_KIND = {torch.float32: ARGMIN_F32, torch.uint8: ARGMIN_U8, torch.int16: ARGMIN_U16,
@@ -68,8 +80,8 @@ def lbp_forward(variant: int, cost: torch.Tensor, jump: torch.Tensor, edge: torc
         if tuple(jump.shape[1:]) != (4, L, L):
             raise BplError(f"semantic jump must be (1,4,L,L), got {tuple(jump.shape)}")
     else:
-        if tuple(jump.shape) != (4, H, W, L, L):
-            raise BplError(f"pixel jump must be (4,H,W,L,L), got {tuple(jump.shape)}")
+        if tuple(jump.shape) != (_pixel_planes(variant), H, W, L, L):
+            raise BplError(f"pixel jump must be ({_pixel_planes(variant)},H,W,L,L), got {tuple(jump.shape)}")
     if argmin_dtype is None:
         kind = ARGMIN_NONE
         argmin = None
@@ -126,23 +138,23 @@ def lbp_backward(variant: int, jump, edge: torch.Tensor, in_grad: torch.Tensor, 
         _check_input("jump", jump, dim=4)
         grad_jump = torch.empty((B, 4, L, L), dtype=torch.float32, device=dev)
     else:
-        grad_jump = torch.empty((4, H, W, L, L), dtype=torch.float32, device=dev)
+        grad_jump = torch.empty((_pixel_planes(variant), H, W, L, L), dtype=torch.float32, device=dev)
     grad_cost = torch.empty((B, H, W, L), dtype=torch.float32, device=dev)
-    grad_edge = None if variant == LBP_SEM_PIXEL else torch.empty(tuple(edge.shape), dtype=torch.float32, device=dev)
+    grad_edge = None if _pixel(variant) else torch.empty(tuple(edge.shape), dtype=torch.float32, device=dev)
     need = lbp_backward_workspace_bytes(B, H, W, L)
     if workspace is None or workspace.numel() * workspace.element_size() < need:
         workspace = torch.empty(need, dtype=torch.uint8, device=dev)
     if mode == "exact":
         grad_messages = torch.empty_like(messages)
         st = _timed("lbp_backward", lambda: lib().bpl_lbp_backward_exact(
-            variant, _ptr(jump) if variant != LBP_SEM_PIXEL else None, _ptr(edge), _ptr(in_grad),
+            variant, _ptr(jump) if not _pixel(variant) else None, _ptr(edge), _ptr(in_grad),
             _ptr(messages), _ptr(argmin), kind, _ptr(scale), _ptr(grad_cost), _ptr(grad_jump),
             _ptr(grad_edge), _ptr(grad_messages), _ptr(workspace), workspace.numel() * workspace.element_size(),
             B, H, W, L, Lv, jb, edge.shape[0], _stream(messages)))
         check(st, "bpl_lbp_backward_exact")
         return grad_cost, grad_jump, grad_edge, grad_messages
     st = _timed("lbp_backward", lambda: lib().bpl_lbp_backward(
-        variant, _ptr(jump) if variant != LBP_SEM_PIXEL else None, _ptr(edge), _ptr(in_grad),
+        variant, _ptr(jump) if not _pixel(variant) else None, _ptr(edge), _ptr(in_grad),
         _ptr(messages), _ptr(argmin), kind, _ptr(scale), _ptr(grad_cost), _ptr(grad_jump),
         _ptr(grad_edge), _ptr(workspace), workspace.numel() * workspace.element_size(),
         B, H, W, L, Lv, jb, edge.shape[0], _stream(messages)))
@@ -310,10 +322,10 @@ def lbp_forward_f16(variant: int, cost_h: torch.Tensor, jump: torch.Tensor, edge
     if variant == LBP_STEREO:
         _check_input("jump", jump, dim=5)
         Lv, jb = jump.shape[2], jump.shape[0]
-    elif variant == LBP_SEM_PIXEL:
+    elif _pixel(variant):
         _check_input("jump", jump, dtype=torch.float16, dim=5)
-        if tuple(jump.shape) != (4, H, W, L, Lp):
-            raise BplError(f"pixel jump must be (4,H,W,L,Lp) half, got {tuple(jump.shape)}")
+        if tuple(jump.shape) != (_pixel_planes(variant), H, W, L, Lp):
+            raise BplError(f"pixel jump must be ({_pixel_planes(variant)},H,W,L,Lp) half, got {tuple(jump.shape)}")
     else:
         raise BplError("FP16 storage serves the stereo and pixel variants")
     # argmin_dtype=None: no argmin is written (inference)
@@ -349,8 +361,8 @@ def lbp_backward_f16(variant: int, jump, edge: torch.Tensor, in_grad_h: torch.Te
         Lv, jb = jump.shape[2], jump.shape[0]
         grad_jump = torch.empty((jb, 4, Lv, H, W), dtype=torch.float32, device=dev)
         grad_edge = torch.empty(tuple(edge.shape), dtype=torch.float32, device=dev)
-    elif variant == LBP_SEM_PIXEL:
-        grad_jump = torch.empty((4, H, W, L, L), dtype=torch.float32, device=dev)
+    elif _pixel(variant):
+        grad_jump = torch.empty((_pixel_planes(variant), H, W, L, L), dtype=torch.float32, device=dev)
         grad_edge = None
     else:
         raise BplError("FP16 storage serves the stereo and pixel variants")
@@ -411,16 +423,16 @@ def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.T
         _check_input("jump", jump, dim=4)
         grad_jump = torch.empty((B, 4, L, L), dtype=torch.float32, device=dev)
     else:
-        grad_jump = torch.empty((4, H, W, L, L), dtype=torch.float32, device=dev)
+        grad_jump = torch.empty((_pixel_planes(variant), H, W, L, L), dtype=torch.float32, device=dev)
     grad_cost = torch.empty((B, H, W, Ls), dtype=torch.float32, device=dev)
-    grad_edge = None if variant == LBP_SEM_PIXEL else torch.empty(tuple(edge.shape), dtype=torch.float32, device=dev)
+    grad_edge = None if _pixel(variant) else torch.empty(tuple(edge.shape), dtype=torch.float32, device=dev)
     need = P * lbp_backward_workspace_bytes(B, H, W, Ls)
     if workspace is None or workspace.numel() * workspace.element_size() < need:
         workspace = torch.empty(need, dtype=torch.uint8, device=dev)
     fn = lib().bpl_lbp_backward_passes_f16 if half else lib().bpl_lbp_backward_passes
     name = "lbp_backward_f16" if half else "lbp_backward"
     st = _timed(name, lambda: fn(
-        variant, _ptr(jump) if variant != LBP_SEM_PIXEL else None, _ptr(edge), _ptr(in_grad), g_bstride, g_sstride,
+        variant, _ptr(jump) if not _pixel(variant) else None, _ptr(edge), _ptr(in_grad), g_bstride, g_sstride,
         _ptr(messages), _ptr(argmins), kind, _ptr(scales), _ptr(grad_cost), _ptr(grad_jump), _ptr(grad_edge), _ptr(workspace),
         workspace.numel() * workspace.element_size(), B, H, W, L, Lv, jb, edge.shape[0], P, _stream(messages)))
     check(st, "bpl_lbp_backward_passes")

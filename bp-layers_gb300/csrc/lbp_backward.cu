@@ -58,7 +58,11 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
                       int B, int H, int W, int L, int Lv, int jump_batch, int edge_batch, void* stream,
                       float* grad_messages = nullptr, int reps = 1, int64_t g_bstride = -1,
                       int64_t g_sstride = -1) {
-  BPL_REQUIRE(variant >= 0 && variant <= 2, "lbp_backward: unknown variant %d", variant);
+  BPL_REQUIRE(variant >= 0 && variant <= 3, "lbp_backward: unknown variant %d", variant);
+  // the pixel variant with the layer's two pairwise planes: same kernels, a
+  // gradient of the planes' layout
+  const int planes2 = (variant == BPL_LBP_SEM_PIXEL_LAYER) ? 1 : 0;
+  if (planes2) variant = BPL_LBP_SEM_PIXEL;
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1, "lbp_backward: bad shape B=%d H=%d W=%d", B, H, W);
   BPL_REQUIRE(H <= 65535 && W <= 65535, "lbp_backward: H and W must be <= 65535");
   BPL_REQUIRE(L >= 1 && L <= 1024, "lbp_backward: L=%d outside [1, 1024]", L);
@@ -84,7 +88,7 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   size_t gj_elems;
   if (variant == BPL_LBP_STEREO) gj_elems = static_cast<size_t>(jump_batch) * 4 * Lv * HW;
   else if (variant == BPL_LBP_SEM_GLOBAL) gj_elems = static_cast<size_t>(B) * 4 * L * L;
-  else gj_elems = static_cast<size_t>(4) * HW * L * L;
+  else gj_elems = static_cast<size_t>(planes2 ? 2 : 4) * HW * L * L;
   BPL_CUDA_TRY(cudaMemsetAsync(grad_cost, 0, sizeof(float) * B * HW * Ls, s), "lbp_backward: memset");
   BPL_CUDA_TRY(cudaMemsetAsync(grad_jump, 0, sizeof(float) * gj_elems, s), "lbp_backward: memset");
   if (grad_edge)
@@ -116,6 +120,7 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   a.jb = jump_batch;
   a.eb = edge_batch;
   a.argmin_kind = argmin_kind;
+  a.planes2 = planes2;
   const int am_size = (argmin_kind == BPL_ARGMIN_U8) ? 1 : (argmin_kind == BPL_ARGMIN_U16 ? 2 : 4);
   if (storage == 0) {
     a.lrow = bwd::a4(L);

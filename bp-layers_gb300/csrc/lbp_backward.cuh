@@ -82,6 +82,12 @@ struct BwdArgs {
   int lrow;
   int vec4;     // float rows are 16-byte sized: bulk copies
   int am_bulk;  // the argmin row is 16-byte sized too: staged with the floats
+  // pixel variant: grad_jump is the layer's (2,H,W,L,L) LR / UD planes; the
+  // gradient of direction RL goes to the LR matrix of the pixel to the left,
+  // transposed, DU to the UD matrix above, transposed, and the zero matrix
+  // of a first RL / DU sender receives none (message_passing_op_pw_pixel.py:
+  // 47-51)
+  int planes2;
 };
 
 constexpr int kBwdRingCpAsync = 4;
@@ -451,9 +457,14 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS |
           if (VARIANT == BPL_LBP_SEM_GLOBAL) {
             sm.jacc[s * L + t] += w * tot;  // distinct t per lane: no conflict
             ge += __ldg(a.jump + (static_cast<int64_t>(fd) * L + s) * L + t) * tot;
-          } else {
+          } else if (!a.planes2) {
             // (4,H,W,L,L) has no batch axis: batch items accumulate
             atomicAdd(a.grad_jump + ((static_cast<int64_t>(fd) * HW + p) * L + s) * L + t, w * tot);
+          } else if (!(fd & 1)) {
+            atomicAdd(a.grad_jump + ((static_cast<int64_t>(fd >> 1) * HW + p) * L + s) * L + t, w * tot);
+          } else if (fd == RIGHT ? (p % a.W != 0) : (p >= a.W)) {
+            const int pp = p - (fd == RIGHT ? 1 : a.W);
+            atomicAdd(a.grad_jump + ((static_cast<int64_t>(fd >> 1) * HW + pp) * L + t) * L + s, w * tot);
           }
         }
       }

@@ -3,6 +3,7 @@
 
 namespace bpl {
 __device__ int g_bpl_error = 0;
+__device__ __align__(16) float g_zero_pairwise[96 * 96];
 }  // namespace bpl
 
 
@@ -14,7 +15,11 @@ namespace {
 int lbp_forward_impl(int storage, int variant, const void* cost, const void* jump, const float* edge,
                      void* messages, void* argmin, int argmin_kind, float* scale, int B, int H, int W, int L,
                      int Lv, int jump_batch, int edge_batch, int delta, void* stream) {
-  BPL_REQUIRE(variant >= 0 && variant <= 2, "lbp_forward: unknown variant %d", variant);
+  BPL_REQUIRE(variant >= 0 && variant <= 3, "lbp_forward: unknown variant %d", variant);
+  // the pixel variant with the layer's two pairwise planes: same kernels,
+  // the shift and transpose applied when a matrix is staged
+  const int planes2 = (variant == BPL_LBP_SEM_PIXEL_LAYER) ? 1 : 0;
+  if (planes2) variant = BPL_LBP_SEM_PIXEL;
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1, "lbp_forward: bad shape B=%d H=%d W=%d", B, H, W);
   BPL_REQUIRE(H <= 65535 && W <= 65535, "lbp_forward: H and W must be <= 65535");
   BPL_REQUIRE(L >= 1 && L <= 1024, "lbp_forward: L=%d outside [1, 1024]", L);
@@ -49,6 +54,7 @@ int lbp_forward_impl(int storage, int variant, const void* cost, const void* jum
   a.eb = edge_batch;
   a.delta = delta;
   a.argmin_kind = argmin_kind;
+  a.planes2 = planes2;
   a.lrow = align4(L);
   if (storage == 0) {
     a.Ls = L;

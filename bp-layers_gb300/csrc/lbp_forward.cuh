@@ -72,6 +72,11 @@ struct FwdArgs {
   int lrow;   // unused
   int lmat;   // elements of the per-pixel pairwise matrix in a stage (pixel variant), else 0
   int vec4;   // rows are 16-byte sized: use bulk copies
+  // pixel variant: the pairwise input is the layer's (2,H,W,L,Lm) LR / UD
+  // planes; direction RL reads the LR matrix of the pixel to its left,
+  // transposed, DU the UD matrix of the pixel above, transposed
+  // (message_passing_op_pw_pixel.py:27-38)
+  int planes2;
 };
 
 // exp/log of the message normalisation with the reference's results
@@ -162,8 +167,14 @@ struct Chain {
   T* slot_out;         // slot written at the receiver (= the incoming chain slot)
   int64_t out_off;     // element offset of slot_out within the messages tensor
   const T* pjump;      // per-pixel pairwise matrices of this direction (pixel variant)
+  int pshift;          // pixel offset of a sender's matrix (-1 or -W for the layer's planes)
+  int ps, pt;          // strides of sender / receiver label in a staged matrix
   int t0, cnt;         // first label of this warp; labels it copies per row
 };
+
+// a zero L x L pairwise matrix (L <= 96, float or half), read by the first
+// sender of the RL / DU directions with the layer's pairwise planes
+extern __device__ __align__(16) float g_zero_pairwise[96 * 96];
 
 // Issues ring slot `st` for step i: the warp's labels [t0, t0+cnt) of the
 // sender's cost and cross-direction messages (+ the pixel's pairwise matrix,
@@ -177,7 +188,12 @@ __device__ __forceinline__ void issue_slot(const FwdArgs& a, const Chain<T>& c, 
   const T* src0 = c.cost + po;
   const T* src1 = c.slot_a + po;
   const T* src2 = c.slot_b + po;
-  const T* src3 = (VARIANT == BPL_LBP_SEM_PIXEL) ? c.pjump + pin * a.L * a.Lm : nullptr;
+  // the first sender of a shifted direction reads the zero matrix (the
+  // layer's shifted tensor is zero there)
+  const T* src3 = (VARIANT == BPL_LBP_SEM_PIXEL)
+                      ? ((c.pshift != 0 && i == 0) ? reinterpret_cast<const T*>(g_zero_pairwise)
+                                                   : c.pjump + (pin + c.pshift) * a.L * a.Lm)
+                      : nullptr;
   if (a.vec4) {
     if (lane == 0) {
       const uint32_t rb = static_cast<uint32_t>(c.cnt) * static_cast<uint32_t>(sizeof(T));
@@ -418,8 +434,14 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
   c.out_off = (static_cast<int64_t>(c.n) * 4 + od) * HWL;
   c.slot_out = static_cast<T*>(a.msgs) + c.out_off;
   c.pjump = (VARIANT == BPL_LBP_SEM_PIXEL)
-                ? static_cast<const T*>(a.jump) + static_cast<int64_t>(c.dir) * HW * L * a.Lm
+                ? static_cast<const T*>(a.jump) + static_cast<int64_t>(a.planes2 ? (c.dir >> 1) : c.dir) * HW * L * a.Lm
                 : nullptr;
+  {
+    const bool tr = (VARIANT == BPL_LBP_SEM_PIXEL) && a.planes2 && (c.dir & 1);
+    c.pshift = tr ? ((c.dir == LEFT || c.dir == RIGHT) ? -1 : -a.W) : 0;
+    c.ps = tr ? 1 : a.Lm;
+    c.pt = tr ? a.Lm : 1;
+  }
   c.t0 = 32 * KW * wic;
   // label validity: with K = ceil(L/32) (the K <= 8 instantiations are
   // dispatched exactly) only the last slot of a one-warp scanline can hold
@@ -593,7 +615,7 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
             } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
               f = __ldg(gjump + s * L + t);
             } else {
-              f = ldf<T>(stg[3 * lroww + s * a.Lm + t]);
+              f = ldf<T>(stg[3 * lroww + s * c.ps + t * c.pt]);
             }
             const float nm = __fmaf_rn(f, w, cs.hs[s]);
             m = fminf(m, nm);
@@ -636,7 +658,7 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
       } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
         L2 = __ldg(gjump + (L - 1));
       } else {
-        L2 = ldf<T>(stg[3 * lroww + (L - 1)]);
+        L2 = ldf<T>(stg[3 * lroww + (L - 1) * c.pt]);
       }
       // The global candidate needs only the minimum value of h, which any
       // reduction order gives exactly.
@@ -838,7 +860,7 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
               } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
                 f = __ldg(gjump + s * L + t);
               } else {
-                f = ldf<T>(stg[3 * lroww + s * a.Lm + t]);
+                f = ldf<T>(stg[3 * lroww + s * c.ps + t * c.pt]);
               }
               const float nm = __fmaf_rn(f, w, cs.hs[s]);
               if (nm <= m) {

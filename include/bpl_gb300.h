@@ -42,6 +42,12 @@ extern "C" {
 #define BPL_LBP_STEREO 0      /* ops/lbp_stereo            */
 #define BPL_LBP_SEM_GLOBAL 1  /* ops/lbp_semantic_pw       */
 #define BPL_LBP_SEM_PIXEL 2   /* ops/lbp_semantic_pw_pixel */
+/* ops/lbp_semantic_pw_pixel with the layer's input instead of the op's: the
+ * pairwise tensor is (2,H,W,L,L) (LR and UD planes) and the kernels apply the
+ * shift and transpose that LBPMinSumFunction.forward materialises as
+ * (4,H,W,L,L) (message_passing_op_pw_pixel.py:27-38); grad_jump is
+ * (2,H,W,L,L), the fold of its backward (:47-51). */
+#define BPL_LBP_SEM_PIXEL_LAYER 3
 
 /* argmin storage */
 #define BPL_ARGMIN_NONE 0
