@@ -678,8 +678,9 @@ def run_ncu_case(args):
     (cost 100 MB, messages 400 MB: larger than L2, well under the capture
     size limit), the exact adjoint's message-gradient assembly, the belief
     epilogue, SAD at 384x512 C=64 D=192, the flow SAD at 384x512 C=32,
-    window +-32, the coarse-to-fine glue into 256x512x192 and the slot
-    broadcast of a 256x512x192 volume."""
+    window +-32, the coarse-to-fine glue into 256x512x192, the slot
+    broadcast of a 256x512x192 volume and the semantic pixel-pairwise
+    forward at 512x1024, L=19 (the layer's two pairwise planes)."""
     import torch
     from bpl_gb300 import ops
     import cases
@@ -697,6 +698,10 @@ def run_ncu_case(args):
     g1 = torch.randn((1, 32, 384, 512), device=dev)
     bc = torch.rand((1, h // 2, w // 2, L // 2), device=dev)
     pvl = torch.rand((1, h, w, L), device=dev)
+    pcost = -torch.softmax(torch.randn((1, 2 * h, 2 * w, 19), device=dev), dim=-1)
+    pjp = torch.rand((2, 2 * h, 2 * w, 19, 19), device=dev)
+    pedge = torch.ones((1, 4, 2 * h, 2 * w), device=dev)
+    pm = torch.zeros((1, 4, 2 * h, 2 * w, 19), device=dev)
     for it in range(2):
         if it == 1:
             torch.cuda.synchronize()
@@ -712,6 +717,7 @@ def run_ncu_case(args):
         ops.flow_backward(g0, g1, 64, cu, cv, us, vs)
         ops.upsample_add_beliefs(bc, pvl, 0.5)
         ops.broadcast_slots(cost)
+        ops.lbp_forward(ops.LBP_SEM_PIXEL_LAYER, pcost, pjp, pedge, pm, 19, argmin_dtype=torch.uint8)
         torch.cuda.synchronize()
     torch.cuda.profiler.stop()
     print(json.dumps({"ncu_case": f"{h}x{w}x{L}", "updates_per_pass": L * edges(h, w)}))
