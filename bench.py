@@ -149,9 +149,11 @@ def run_ours(args):
         mp._L2.fill_(0.5)
     prob.requires_grad_(True)
 
-    def step(p, e, g):
+    def step(p, e, g, before_backward=None):
         messages = torch.zeros((1, 4, H, W, L), device=dev, requires_grad=True)
         beliefs, _ = mp(p, e, None, None, messages)
+        if before_backward is not None:
+            before_backward()
         beliefs.backward(g)
         return beliefs
 
@@ -186,8 +188,11 @@ def run_ours(args):
     # Every step copies its inputs from pinned host memory and its results
     # (cost gradient, disparity map) back; the copies run on their own
     # streams, double-buffered, so step i+1's inputs arrive and step i-1's
-    # results leave while step i computes.  The timed region spans the first
-    # input copy to the last result copy.
+    # results leave while step i computes.  The forward waits for the
+    # probability volume and edge weights only; the upstream gradient has
+    # its own event, which the backward waits for (it lands while the
+    # forward runs).  The timed region spans the first input copy to the
+    # last result copy.
     prob_h = prob.detach().cpu().pin_memory()
     edge_h = edge.cpu().pin_memory()
     up_h = upstream.cpu().pin_memory()
@@ -199,6 +204,7 @@ def run_ours(args):
     bufs = [(torch.empty(prob_h.shape, device=dev), torch.empty(edge_h.shape, device=dev),
              torch.empty(up_h.shape, device=dev)) for _ in range(2)]
     in_ready = [torch.cuda.Event() for _ in range(2)]
+    up_ready = [torch.cuda.Event() for _ in range(2)]
     in_free = [torch.cuda.Event() for _ in range(2)]
     out_done = [torch.cuda.Event() for _ in range(2)]
     for ev in in_free:
@@ -208,9 +214,11 @@ def run_ours(args):
         k = i % 2
         with torch.cuda.stream(cin):
             cin.wait_event(in_free[k])  # step i-2 has finished reading buffer k
-            for dst, src in zip(bufs[k], (prob_h, edge_h, up_h)):
-                dst.copy_(src, non_blocking=True)
+            bufs[k][0].copy_(prob_h, non_blocking=True)
+            bufs[k][1].copy_(edge_h, non_blocking=True)
             in_ready[k].record(cin)
+            bufs[k][2].copy_(up_h, non_blocking=True)
+            up_ready[k].record(cin)
 
     def e2e_run(n):
         issue_inputs(0)
@@ -220,7 +228,7 @@ def run_ours(args):
                 issue_inputs(i + 1)
             stream.wait_event(in_ready[k])
             p = bufs[k][0].detach().requires_grad_(True)
-            beliefs = step(p, bufs[k][1], bufs[k][2])
+            beliefs = step(p, bufs[k][1], bufs[k][2], before_backward=lambda: stream.wait_event(up_ready[k]))
             disp = torch.argmax(beliefs.detach(), dim=3, keepdim=True)
             in_free[k].record(stream)
             gr = p.grad
