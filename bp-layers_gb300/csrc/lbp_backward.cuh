@@ -146,13 +146,19 @@ template <>
 __device__ __forceinline__ float bldf<__half>(__half v) { return __half2float(v); }
 
 // The vertical phase (one scanline per column) runs 2-warp blocks, 9 of
-// them resident per SM, so that a full-width image's columns fit one wave;
-// the horizontal phase is latency-bound and keeps its registers.
+// them resident per SM (18 warps).  The horizontal phase runs 4-warp blocks,
+// 4 resident per SM (registers capped near 128): with the passes of an
+// iteration loop batched its scanlines number 2 * passes * rows (2256 at
+// 3 x 376 rows), which 16 warps per SM hold in one wave; uncapped (161
+// registers, 12 warps per SM) the last quarter ran as a second wave of
+// full-length chains.
 template <bool CROSS, int K>
 constexpr int bwd_warps_per_block() { return (CROSS || K > 8) ? 4 : 2; }
+template <bool CROSS, int K>
+constexpr int bwd_min_blocks() { return K > 8 ? 1 : (CROSS ? 4 : 9); }
 
 template <int K, int VARIANT, int LV, bool CROSS, typename T>
-__global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), (CROSS || K > 8) ? 1 : 9)
+__global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_blocks<CROSS, K>())
     lbp_backward_kernel(BwdArgs a) {
   using namespace bwd;
   extern __shared__ __align__(16) float smem[];

@@ -138,3 +138,27 @@ def test_flow_window_limit_raises():
     f = torch.zeros((1, 2, 4, 4), device=dev)
     with pytest.raises(ops.BplError):
         ops.flow_forward(f, f, 256)
+
+
+def test_flow_backward_entry_allocating_its_scratch():
+    """bpl_flow_backward (scratch allocated stream-ordered inside the call)
+    gives the results of bpl_flow_backward_ws."""
+    import ctypes
+    from bpl_gb300 import ops, _lib
+    g = cases.rng(61)
+    B, C, H, W, sws = 1, 8, 9, 14, 6
+    dev = torch.device("cuda:0")
+    f0 = torch.from_numpy(g.normal(0, 1, size=(B, C, H, W)).astype(np.float32)).to(dev)
+    f1 = torch.from_numpy(g.normal(0, 1, size=(B, C, H, W)).astype(np.float32)).to(dev)
+    cu, cv, us, vs = ops.flow_forward(f0, f1, sws)
+    gu, gv = torch.randn_like(cu), torch.randn_like(cv)
+    d0, d1 = ops.flow_backward(f0, f1, sws, gu, gv, us, vs)
+    e0, e1 = torch.empty_like(f0), torch.empty_like(f1)
+    P = ctypes.c_void_p
+    st = _lib.lib().bpl_flow_backward(P(f0.data_ptr()), P(f1.data_ptr()), P(gu.data_ptr()), P(gv.data_ptr()),
+                                      P(us.data_ptr()), P(vs.data_ptr()), P(e0.data_ptr()), P(e1.data_ptr()),
+                                      B, C, H, W, sws, P(torch.cuda.current_stream().cuda_stream))
+    assert st == 0
+    torch.cuda.synchronize()
+    assert torch.equal(e0, d0)
+    assert float((e1 - d1).abs().max()) <= 1e-5 * max(float(d1.abs().max()), 1.0)
