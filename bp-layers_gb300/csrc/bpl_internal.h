@@ -36,5 +36,8 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 int sm_count();
 // Opt-in shared memory per block of the current device.
 int max_smem_optin();
+// Shared memory per SM and the runtime's reservation per resident block.
+int smem_per_sm();
+int smem_reserved_per_block();
 
 }  // namespace bpl

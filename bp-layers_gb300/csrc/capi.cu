@@ -30,6 +30,8 @@ namespace {
 struct DevProps {
   int sms = 0;
   int smem_optin = 0;
+  int smem_sm = 0;
+  int smem_reserved = 0;
 };
 std::mutex g_props_mu;
 DevProps g_props[64];
@@ -43,6 +45,8 @@ const DevProps& props() {
   if (!g_props_ok[dev]) {
     cudaDeviceGetAttribute(&g_props[dev].sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&g_props[dev].smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&g_props[dev].smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&g_props[dev].smem_reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
     g_props_ok[dev] = true;
   }
   return g_props[dev];
@@ -51,6 +55,8 @@ const DevProps& props() {
 
 int sm_count() { return props().sms > 0 ? props().sms : 152; }
 int max_smem_optin() { return props().smem_optin > 0 ? props().smem_optin : 48 * 1024; }
+int smem_per_sm() { return props().smem_sm > 0 ? props().smem_sm : 228 * 1024; }
+int smem_reserved_per_block() { return props().smem_reserved > 0 ? props().smem_reserved : 1024; }
 
 }  // namespace bpl
 

@@ -525,7 +525,10 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
         ok = mbar_wait_bounded(&sm.bars[grp], (par >> grp) & 1u);
         par ^= 1u << grp;
       } else {
-        cp_async_wait<kRingCpAsync - 1>();  // groups 0..i have landed
+        // groups 0..i have landed (one group per step, a.ns in flight)
+        if (a.ns == 4) cp_async_wait<3>();
+        else if (a.ns == 3) cp_async_wait<2>();
+        else cp_async_wait<1>();
       }
       __syncwarp();
     }
@@ -1043,8 +1046,21 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
 
 // Host-side launch of one phase for one (K, variant, NW) instantiation.
 template <int K, int V, int NW, typename T>
-int launch_phase(const FwdArgs& a, cudaStream_t stream) {
+int launch_phase(const FwdArgs& a0, cudaStream_t stream) {
+  FwdArgs a = a0;
   const int lroww = 32 * (K / NW);
+  if (V == BPL_LBP_SEM_PIXEL && NW == 1 && a.nchains > kHiOccChainsPerSm * sm_count()) {
+    // one-warp blocks: the deepest ring (4..2 steps) whose shared memory lets
+    // every scanline of the phase be resident at once; a second, partial
+    // wave of full-length scanlines costs more than a shallower prefetch
+    for (int ns = a.ns; ns >= 2; --ns) {
+      const size_t pc = 4 * (static_cast<size_t>(chain_smem_floats(K)) +
+                             static_cast<size_t>(warp_smem_floats(ns, lroww, a.lmat, a.Lv, sizeof(T))));
+      const int per_sm = std::min(32, static_cast<int>(smem_per_sm() / (pc + smem_reserved_per_block())));
+      a.ns = ns;
+      if (static_cast<int64_t>(per_sm) * sm_count() >= a.nchains) break;
+    }
+  }
   const size_t per_chain = 4 * (static_cast<size_t>(chain_smem_floats(K)) +
                                 static_cast<size_t>(NW) * warp_smem_floats(a.ns, lroww, a.lmat, a.Lv, sizeof(T)));
   // a phase with more scanlines than about 8 warps per SM runs 1-warp

@@ -111,3 +111,25 @@ def test_semantic_pixel_layer_gradient_matches_materialised():
     ref = _fold2(gref)
     tol = 1e-5 * max(float(ref.abs().max()), 1.0)
     assert float((jp.grad - ref).abs().max()) <= tol
+
+
+def test_wide_batch_shallow_ring_matches_oracle():
+    """2 x 1024 columns: the vertical phase runs more scanlines than one
+    wave holds with a 4-step ring, so it runs a shallower one; results are
+    those of the oracle."""
+    import oracle
+    from bpl_gb300 import ops
+    dev = torch.device("cuda:0")
+    g = cases.rng(54)
+    B, H, W, L = 2, 5, 1024, 19
+    cost = cases.random_cost(g, B, H, W, L)
+    jp = g.uniform(0.0, 1.5, size=(2, H, W, L, L)).astype(np.float32)
+    edge = cases.edge_weights(g, B, H, W)
+    j4 = _shift4(torch.from_numpy(jp)).numpy()
+    m, am, sc = ops.lbp_forward(ops.LBP_SEM_PIXEL_LAYER, torch.from_numpy(cost).to(dev), torch.from_numpy(jp).to(dev),
+                                torch.from_numpy(edge).to(dev), torch.zeros((B, 4, H, W, L), device=dev), L,
+                                argmin_dtype=torch.float32)
+    rm, ram, rsc = oracle.lbp_forward(2, cost, j4, edge, np.zeros((B, 4, H, W, L), np.float32), L)
+    np.testing.assert_array_equal(m.cpu().numpy(), rm)
+    np.testing.assert_array_equal(am.cpu().numpy(), ram)
+    np.testing.assert_array_equal(sc.cpu().numpy(), rsc)
