@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (oracle/bpl_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY.  Imported by tests/, by __graft_entry__.smoke() and
-by bench.py's CPU-baseline leg, always as the checker or the timed CPU
+by bench.py's CPU-baseline leg, always as the test reference or the timed CPU
 baseline, never as a code path of the product.
 
 Each function mirrors one reference op (file:line citations are in
