@@ -68,8 +68,12 @@ constexpr int kPXG = kTX / kPX;  // pixel groups per block
 // leading pad of an f1 row: (window start + pad) % 4 == 0 for every thread
 __host__ __device__ inline int sad_pad(int dhi, int dlo) { return ((7 - (dhi - dlo)) % 4 + 4) % 4; }
 
-// grid (ceil(W/kTX), H, B); block kPXG x (D/kPD rounded up) threads
-__global__ void __launch_bounds__(512) sad_forward_kernel(SadArgs a) {
+// grid (ceil(W/kTX), H, B); block kPXG x (D/kPD rounded up) threads.
+// MAXT/MINB: blocks of up to 384 threads run with registers capped (80, no
+// spills) so that 2-3 blocks stay resident per SM and one block's chunk
+// barrier does not idle the SM; 512-thread blocks (D > 192) keep theirs.
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) sad_forward_kernel(SadArgs a) {
   extern __shared__ __align__(16) float sm[];
   const int n = blockIdx.z, y = blockIdx.y, x0 = blockIdx.x * kTX;
   const int span = kTX + (a.dhi - a.dlo);      // f1 columns a block can match
@@ -374,15 +378,19 @@ extern "C" int bpl_sad_forward(const float* f0, const float* f1, float* out, int
   const int span = kTX + (a.dhi - a.dlo);
   const int pad = a.unit_step ? sad_pad(a.dhi, a.dlo) : 0;
   const size_t smem = 2 * sizeof(float) * kCChunk * (kTX + ((pad + span + 3) & ~3));  // two chunk buffers
-  if (smem > 48 * 1024) {
-    BPL_REQUIRE(static_cast<int>(smem) <= max_smem_optin(), "sad_forward: disparity span too large");
-    BPL_CUDA_TRY(cudaFuncSetAttribute(sad_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(smem)), "cudaFuncSetAttribute");
-  }
-  dim3 grid((W + kTX - 1) / kTX, H, B);
-  sad_forward_kernel<<<grid, threads, smem, as_stream(stream)>>>(a);
-  BPL_CUDA_TRY(cudaGetLastError(), "sad_forward launch");
-  return BPL_OK;
+  BPL_REQUIRE(static_cast<int>(smem) <= max_smem_optin(), "sad_forward: disparity span too large");
+  auto launch = [&](auto kern) -> int {
+    if (smem > 48 * 1024)
+      BPL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+                   "cudaFuncSetAttribute");
+    dim3 grid((W + kTX - 1) / kTX, H, B);
+    kern<<<grid, threads, smem, as_stream(stream)>>>(a);
+    BPL_CUDA_TRY(cudaGetLastError(), "sad_forward launch");
+    return BPL_OK;
+  };
+  if (threads <= 256) return launch(sad_forward_kernel<256, 3>);
+  if (threads <= 384) return launch(sad_forward_kernel<384, 2>);
+  return launch(sad_forward_kernel<512, 1>);
 }
 
 extern "C" int bpl_sad_backward(const float* f0, const float* f1, const float* in_grad, float* df0, float* df1,
