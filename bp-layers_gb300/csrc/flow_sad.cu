@@ -329,10 +329,12 @@ struct FlowBwdArgs {
 constexpr int kBwdPx = 8;      // pixels (warps) per block
 constexpr int kBwdUnroll = 8;  // window entries gathered together
 
-// grid (ceil(W/8), H, B); block 256: warp w = pixel x0 + w, lane = channel.
+// grid (ceil(W/8), H, B); block 256: warp w = pixel x0 + w, lane = channel;
+// registers capped for 4 resident blocks per SM (the gathers are
+// latency-bound: more warps in flight).
 // Offsets inside one batch item are 32-bit (H*W*C < 2^31, checked by the
 // host).
-__global__ void __launch_bounds__(256, 3) flow_backward_kernel(FlowBwdArgs a) {
+__global__ void __launch_bounds__(256, 4) flow_backward_kernel(FlowBwdArgs a) {
   __shared__ float d0s[32][kBwdPx + 1];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int n = blockIdx.z, y = blockIdx.y, x0 = blockIdx.x * kBwdPx;
