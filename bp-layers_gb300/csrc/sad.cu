@@ -235,7 +235,7 @@ __device__ __forceinline__ void sad_term(float& acc, float diff, float g) {
 // is, which is never -0).  Each thread slides a 4-value window over the
 // staged rows, so a disparity costs it one new value per row and one
 // broadcast 16-byte load per gradient table.
-__global__ void __launch_bounds__(256, 1) sad_backward_kernel(SadBwdArgs a) {
+__global__ void __launch_bounds__(256, 3) sad_backward_kernel(SadBwdArgs a) {
   // two buffers: chunk ci + 1 lands (cp.async) while chunk ci is summed
   __shared__ float f1s[2][kBCH * kBFS];   // f1[c, x0 - d0 - 31 + k]
   __shared__ float f0s[2][kBCH * kBFS];   // f0[c, x0 + d0 + k]
