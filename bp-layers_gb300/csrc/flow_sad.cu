@@ -17,14 +17,16 @@
 // Forward (FP32-issue bound: K*K*C abs-diff-adds per pixel).  A block owns
 // 32 pixels of one row and every displacement u; it walks the window rows v
 // in order.  For each row the f1 row segment the 32 windows touch is staged
-// in shared memory, channel chunk by channel chunk (cp.async, double
-// buffered), and each thread accumulates a 4 x 4 register tile of (pixel,
-// u) SADs: per channel one 16-byte load of f0, two of f1 and 16 sub+abs-add
-// pairs, channels summed in order (bit-identical SADs).  cv_u is a running
-// minimum over the rows in registers (v ascending, strict <); cv_v is the
-// minimum over u of the row, taken per thread over its 4 displacements and
-// then across the threads in u order (strict < keeps the first index).  The
-// window never sits in shared memory, so any K up to 256 fits.
+// in shared memory, double-buffered, by one bulk copy per channel row behind
+// an mbarrier (16-byte aligned rows) or by 4-byte cp.async, and each thread
+// accumulates a 4 x 4 register tile of (pixel, u) SADs: per channel one
+// 16-byte load of f0, two of f1 and 16 sub+abs-add pairs, channels summed in
+// order (bit-identical SADs).  cv_u is a running minimum over the rows in
+// registers (v ascending, strict <); cv_v is the minimum over u of the row:
+// per thread over its 4 displacements, then over the warp by shuffles and
+// over the warps through a shared table, each step on (value, index) as one
+// 64-bit key that reproduces the first-index strict-< scan.  The window
+// never sits in shared memory, so any K up to 256 fits.
 //
 // Backward.  The four (B,H,W,K) volumes are read once (the reference reads
 // them once per channel).  One warp per pixel, lane = channel: for every
