@@ -15,8 +15,9 @@
 // reference), then writes its 8 disparities of each pixel as two 16-byte
 // stores.  FP32-issue bound (about 29 flop/byte at 376x1240x64x192); the
 // channel chunks are double-buffered (cp.async of chunk i+1 while chunk i is
-// summed), because a 512-thread block leaves one block per SM and a
-// synchronous load per chunk stalled the whole SM.
+// summed), and blocks of up to 384 threads run with registers capped so that
+// 2-3 are resident per SM: one block's chunk barrier then leaves the others
+// issuing (a 512-thread block, D > 192, stays alone on its SM).
 // Backward: lanes are channels and each thread owns 4 pixels; both sums walk
 // the disparities in the reference order (additions of +-g in the same
 // sequence: bit-identical).  Per chunk of 32 disparities the block stages
