@@ -342,6 +342,13 @@ def run_ours(args):
         result["accuracy_vs_fp64_oracle"] = run_accuracy()
     if rank == 0 and world == 1 and not args.no_other:
         result["other_configs"] = run_other_configs()
+    if rank == 0 and world == 1 and not args.no_reference_gpu:
+        try:
+            result.setdefault("other_configs", {})[f"reference_gpu_ops_{H}x{W}x{L}"] = run_reference_gpu_ops(
+                fwd_ms, bwd_ms, ms_max / args.steps)
+        except Exception as exc:  # the reference arm never takes the bench down
+            result.setdefault("other_configs", {})[f"reference_gpu_ops_{H}x{W}x{L}"] = {
+                "unavailable": f"{type(exc).__name__}: {str(exc)[:200]}"}
     traffic = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic):
         with open(traffic) as fh:
@@ -575,8 +582,10 @@ def run_other_configs():
     flow = timed(lambda: ops.flow_forward(f0, f1, 64))
     cu, cv, us, vs = ops.flow_forward(f0, f1, 64)
     flow_b = timed(lambda: ops.flow_backward(f0, f1, 64, cu, cv, us, vs))
+    flow_rate = 384 * 512 * 65 * 65 * 32 / (flow / 1e3)
     out["flow_sad_384x512_C32_w65"] = {"forward_ms": flow, "backward_ms": flow_b,
-                                       "forward_G_absdiff_per_s": 384 * 512 * 65 * 65 * 32 / (flow / 1e3) / 1e9}
+                                       "forward_G_absdiff_per_s": flow_rate / 1e9,
+                                       "forward_fp32_issue_frac": fp32_issue_frac(flow_rate)}
     del cu, cv, us, vs
     flow2 = timed(lambda: ops.flow_forward(f0, f1, 216), n=1)
     cu, cv, us, vs = ops.flow_forward(f0, f1, 216)
@@ -608,10 +617,84 @@ def run_other_configs():
     sad = timed(lambda: ops.sad_forward(f0, f1, 0, L - 1))
     vol = ops.sad_forward(f0, f1, 0, L - 1)
     sad_b = timed(lambda: ops.sad_backward(f0, f1, 0, L - 1, vol))
+    sad_rate = H * W * L * 64 / (sad / 1e3)
+    # backward: two sign-gather terms (df0 and df1) per volume entry and channel
+    sad_b_rate = 2 * H * W * L * 64 / (sad_b / 1e3)
     out[f"stereo_sad_{H}x{W}_C64_D{L}"] = {"forward_ms": sad, "backward_ms": sad_b,
-                                            "forward_G_absdiff_per_s": H * W * L * 64 / (sad / 1e3) / 1e9,
-                                            "forward_GBps": (4 * 2 * 64 * H * W + 4 * H * W * L) / (sad / 1e3) / 1e9}
+                                            "forward_G_absdiff_per_s": sad_rate / 1e9,
+                                            "forward_fp32_issue_frac": fp32_issue_frac(sad_rate),
+                                            "forward_GBps": (4 * 2 * 64 * H * W + 4 * H * W * L) / (sad / 1e3) / 1e9,
+                                            "backward_G_terms_per_s": sad_b_rate / 1e9}
     return out
+
+
+def run_reference_gpu_ops(ours_fwd_ms, ours_bwd_ms, ours_step_ms):
+    """The reference's own CUDA op (ops/lbp_stereo, rebuilt on this machine
+    from the copy tests/golden/prepare_reference.sh makes under
+    baseline/_ref) timed on the full-size workload at B=1: ITERS in-place
+    forward_minsum passes and ITERS backward_minsum calls, as its layer runs
+    them (message_passing_op_cuda.py:161-168), beside this library's
+    per-pass times.  Reported as unavailable when the copy is absent or does
+    not build within the time limit."""
+    import torch
+    ref_ops = os.path.join(ROOT, "baseline", "_ref", "ops")
+    if not os.path.isdir(ref_ops):
+        return {"unavailable": "reference copy absent (baseline/_ref/ops; tests/golden/prepare_reference.sh)"}
+    t = time.perf_counter()
+    r = subprocess.run([sys.executable, "-c", "import make_golden; make_golden.build_reference(names=['ref_lbp_stereo'])"],
+                       cwd=os.path.join(ROOT, "tests", "golden"), capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        return {"unavailable": "reference build failed: " + r.stderr.strip().splitlines()[-1][:200]}
+    build_s = time.perf_counter() - t
+    import make_golden
+    st = make_golden.load("ref_lbp_stereo")
+    dev = torch.device("cuda", 0)
+    prob, edge, _ = synth_inputs(torch, dev, 0)
+    cost = (-prob).contiguous()
+    jump = torch.zeros((1, 4, 6, H, W), device=dev)
+    jump[:, :, 1] = 0.5
+    jump[:, :, 2] = 0.1
+    jump[:, :, 4] = 0.1
+    jump[:, :, 5] = 0.5
+    gin = torch.randn((1, 4, H, W, L), device=dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def run():
+        m = torch.zeros((1, 4, H, W, L), device=dev)
+        a, b, c = ev(), ev(), ev()
+        a.record()
+        saved = []
+        for _ in range(ITERS):
+            m, am, sc = st.forward_minsum(cost, jump, edge, m, DELTA)
+            saved.append((am, sc))
+        b.record()
+        for am, sc in saved:
+            st.backward_minsum(cost, jump, edge, gin, m, am, sc)
+        c.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b), b.elapsed_time(c)
+
+    run()  # warm-up
+    f, bw = run()
+    step = f + bw
+    return {"op": "ops/lbp_stereo forward_minsum / backward_minsum (the reference's CUDA kernels, built here with "
+                  "nvcc 13 for sm_103)", "B": 1, "H": H, "W": W, "L": L, "iters": ITERS,
+            "reference_forward_pass_ms": f / ITERS, "reference_backward_pass_ms": bw / ITERS,
+            "reference_step_ms": step,
+            "ours_forward_pass_ms": ours_fwd_ms, "ours_backward_pass_ms": ours_bwd_ms,
+            "ours_layer_step_ms": ours_step_ms,
+            "speedup_ops": step / (ITERS * (ours_fwd_ms + ours_bwd_ms)),
+            "speedup_layer_step": step / ours_step_ms, "reference_build_s": build_s}
+
+
+def fp32_issue_frac(absdiff_per_s):
+    """Fraction of the FP32 issue bound of a SAD kernel: each abs-diff term is
+    two FP32 instructions (a subtract and an add of its absolute value), at
+    128 FP32 lanes per SM per clock, at the device's maximum SM clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    bound = sms * 128 * 2.07e9 / 2
+    return absdiff_per_s / bound
 
 
 def cpu_sample_inputs(wc=CPU_CROP_W):
@@ -746,6 +829,8 @@ def main():
     ap.add_argument("--accuracy-only", action="store_true")
     ap.add_argument("--no-other", action="store_true", help="skip the other configurations' op timings")
     ap.add_argument("--other-only", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference's own CUDA op (built from baseline/_ref)")
     ap.add_argument("--serve-requests", type=int, default=40)
     ap.add_argument("--serve-load", type=float, default=4.0,
                     help="offered arrival rate as a multiple of the plain per-request capacity")

@@ -6,6 +6,6 @@ Layout of the package:
   ops.py        torch-tensor wrappers of the C ABI (allocation, checks, stream)
   compat/       drop-in replacements of the reference's extension modules
 """
-from ._lib import BplError, lib, read_device_error  # noqa: F401
+from ._lib import BplError, check_device_error, lib, read_device_error  # noqa: F401
 
-__all__ = ["BplError", "lib", "read_device_error"]
+__all__ = ["BplError", "check_device_error", "lib", "read_device_error"]

@@ -77,7 +77,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         list(ex.map(run, cmds))
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
     run([nvcc, "-shared", "-o", tmp] + objs + [f"-gencode=arch=compute_{ARCH},code=sm_{ARCH}", "-rdc=true",
-                                            "-Xcompiler", "-fPIC", "-lcudart"])
+                                            "-Xcompiler", "-fPIC", "-lcudart", "-ldl"])
     os.replace(tmp, LIB_PATH)
     with open(stamp, "w") as fh:
         fh.write(digest)

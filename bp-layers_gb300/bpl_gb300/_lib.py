@@ -21,6 +21,7 @@ SIGNATURES = {
     "bpl_status_string": [c_int],
     "bpl_last_error": [],
     "bpl_read_device_error": [c_void_p],
+    "bpl_set_wait_limit": [ctypes.c_uint],
     "bpl_lbp_forward": [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p] + [c_int] * 8 + [c_void_p],
     "bpl_lbp_forward_f16": [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p] + [c_int] * 8 + [c_void_p],
     "bpl_lbp_backward_workspace_size": [c_int] * 4,
@@ -75,6 +76,32 @@ def check(status: int, what: str) -> None:
 
 
 def read_device_error() -> int:
+    """Synchronises the current device, returns and clears the device error
+    word (0: no kernel's bounded wait ran out since the last read)."""
     code = ctypes.c_int(0)
     check(lib().bpl_read_device_error(ctypes.byref(code)), "bpl_read_device_error")
     return code.value
+
+
+DEVICE_ERRORS = {1: "a kernel's bounded wait for its staged input ran out (device wait timeout)"}
+
+
+def check_device_error() -> None:
+    """Raises BplError if a kernel launched since the last check reported a
+    device error; the outputs of those launches are then incomplete.  The
+    launches themselves do not synchronise, so callers check at a point
+    where they synchronise anyway (a loss read back to the host, the end of
+    an epoch or of a served batch).  Synchronises the current device."""
+    code = read_device_error()
+    if code:
+        raise BplError("device error %d: %s" % (code, DEVICE_ERRORS.get(code, "unknown")))
+
+
+DEFAULT_WAIT_LIMIT = 1 << 24
+
+
+def set_wait_limit(polls: int | None) -> None:
+    """Poll limit of the kernels' bounded waits on the current device (None:
+    the default; 0: every wait gives up at once).  For tests of the timeout
+    path."""
+    check(lib().bpl_set_wait_limit(DEFAULT_WAIT_LIMIT if polls is None else int(polls)), "bpl_set_wait_limit")

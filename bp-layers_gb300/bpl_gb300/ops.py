@@ -10,7 +10,9 @@ from __future__ import annotations
 
 import torch
 
-from ._lib import BplError, check, lib
+import os
+
+from ._lib import BplError, check, check_device_error, lib, read_device_error, set_wait_limit  # noqa: F401
 
 LBP_STEREO, LBP_SEM_GLOBAL, LBP_SEM_PIXEL = 0, 1, 2
 # the pixel variant fed the layer's (2,H,W,L,L) LR / UD pairwise planes (the
@@ -189,7 +191,23 @@ class timing:
         return {k: [a.elapsed_time(b) for a, b in v] for k, v in self.events.items()}
 
 
+# BPL_CHECK_DEVICE_ERRORS=1: every call made through this module synchronises
+# and checks the device error word afterwards (a debugging mode; by default
+# callers check with check_device_error() at their own synchronisation
+# points).
+_check_each_call = os.environ.get("BPL_CHECK_DEVICE_ERRORS", "0") not in ("", "0")
+
+
 def _timed(name, fn):
+    if _check_each_call:
+        r = _timed_call(name, fn)
+        if r == 0:
+            check_device_error()
+        return r
+    return _timed_call(name, fn)
+
+
+def _timed_call(name, fn):
     if _timing is None:
         return fn()
     a = torch.cuda.Event(enable_timing=True)

@@ -200,6 +200,7 @@ using namespace bpl;
 
 extern "C" int bpl_broadcast_slots(const void* src, void* dst, int B, int64_t row_elems, int elem_bytes,
                                    void* stream) {
+  BPL_TRACE("bpl_broadcast_slots");
   BPL_REQUIRE(src && dst, "broadcast_slots: null pointer");
   BPL_REQUIRE(B >= 1 && B <= 65535 && row_elems >= 1, "broadcast_slots: bad shape");
   BPL_REQUIRE(elem_bytes == 2 || elem_bytes == 4, "broadcast_slots: element size %d not 2 or 4", elem_bytes);
@@ -225,6 +226,7 @@ extern "C" int bpl_broadcast_slots(const void* src, void* dst, int B, int64_t ro
 extern "C" int bpl_beliefs_forward(const void* messages, int messages_half, const float* cost,
                                    const float* temperature, float* beliefs, int B, int H, int W, int L, int Ls,
                                    void* stream) {
+  BPL_TRACE("bpl_beliefs_forward");
   BPL_REQUIRE(messages && cost && beliefs && temperature, "beliefs_forward: null pointer");
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1 && L >= 1 && L <= 1024 && Ls >= L, "beliefs_forward: bad shape");
   if (messages_half)
@@ -238,6 +240,7 @@ extern "C" int bpl_beliefs_backward(const void* messages, int messages_half, con
                                     const float* temperature, const float* beliefs, const float* grad_beliefs,
                                     float* grad_z, float* grad_temperature, int B, int H, int W, int L, int Ls,
                                     void* stream) {
+  BPL_TRACE("bpl_beliefs_backward");
   BPL_REQUIRE(beliefs && grad_beliefs && grad_z && temperature, "beliefs_backward: null pointer");
   BPL_REQUIRE(grad_temperature == nullptr || (messages && cost), "beliefs_backward: null messages/cost");
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1 && L >= 1 && L <= 1024 && Ls >= L, "beliefs_backward: bad shape");

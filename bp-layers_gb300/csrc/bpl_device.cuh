@@ -29,6 +29,13 @@ __host__ __device__ constexpr int np2(int k) {
 // Error word written by kernels whose bounded waits ran out.  Read with
 // bpl_read_device_error().
 extern __device__ int g_bpl_error;
+// Poll limit of the bounded waits (default kWaitLimit; bpl_set_wait_limit
+// lowers it so that a test can make a wait run out).
+extern __device__ unsigned g_bpl_wait_limit;
+constexpr unsigned kWaitLimit = 1u << 24;
+// Poll limit of the drain that waits for a failed kernel's copies in flight
+// (independent of g_bpl_wait_limit: those copies always land).
+constexpr unsigned kDrainLimit = 1u << 20;
 
 enum DeviceError { DEV_ERR_NONE = 0, DEV_ERR_WAIT_TIMEOUT = 1 };
 
@@ -195,11 +202,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Bounded wait: gives up after `limit` polls (each poll may suspend for a
 // hardware-defined interval), raising DEV_ERR_WAIT_TIMEOUT.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit = (1u << 24)) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
   for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   raise_device_error(DEV_ERR_WAIT_TIMEOUT);
   return false;
+}
+// ... with the library's poll limit (g_bpl_wait_limit)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  return mbar_wait_bounded(bar, parity, *static_cast<volatile unsigned*>(&g_bpl_wait_limit));
 }
 
 // 4-byte cp.async (any alignment) with group commit/wait, for rows whose

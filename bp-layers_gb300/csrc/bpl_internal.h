@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -31,6 +33,18 @@ inline int cuda_status(cudaError_t e, const char* where) {
   } while (0)
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// NVTX range over the host-side scope of an entry point or of one sweep
+// phase's launch: named ranges in Nsight Systems / Compute timelines, a few
+// nanoseconds and no dependency when no tool is attached (NVTX v3 is
+// header-only).
+struct TraceRange {
+  explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+  ~TraceRange() { nvtxRangePop(); }
+  TraceRange(const TraceRange&) = delete;
+  TraceRange& operator=(const TraceRange&) = delete;
+};
+#define BPL_TRACE(name) ::bpl::TraceRange bpl_trace_scope_(name)
 
 // Number of SMs of the current device (cached per device).
 int sm_count();

@@ -88,4 +88,10 @@ int bpl_read_device_error(int* code) {
   return BPL_OK;
 }
 
+int bpl_set_wait_limit(unsigned polls) {
+  const unsigned v = polls;
+  BPL_CUDA_TRY(cudaMemcpyToSymbol(bpl::g_bpl_wait_limit, &v, sizeof(unsigned)), "set_wait_limit");
+  return BPL_OK;
+}
+
 }  // extern "C"

@@ -171,6 +171,7 @@ __global__ void __launch_bounds__(MAXT, MINB) flow_forward_kernel(FlowArgs a) {
   if (nstage > 0) issue(0);
   bool failed = false;
   int s = 0;
+  int s_stop = -1;  // the last stage waited for when a wait ran out
   for (int vi = 0; vi < a.K; ++vi) {
     float acc[4][4];
 #pragma unroll
@@ -218,8 +219,13 @@ __global__ void __launch_bounds__(MAXT, MINB) flow_forward_kernel(FlowArgs a) {
           }
         }
         // buffer s & 1 is restaged by issue(s + 2), which the row's closing
-        // barrier orders after this read for the row's last chunk
-        if (ch + 1 < nch) __syncthreads();
+        // barrier orders after this read for the row's last chunk; a wait
+        // that ran out in any thread stops the block before it issues more
+        if (ch + 1 < nch && __syncthreads_or(failed)) {
+          failed = true;
+          s_stop = s;
+          break;
+        }
       }
     }
     // window values (40 where the match is outside the image), the running
@@ -251,6 +257,7 @@ __global__ void __launch_bounds__(MAXT, MINB) flow_forward_kernel(FlowArgs a) {
     }
     // a timed-out wait stops the whole block
     if (__syncthreads_or(failed)) {
+      if (s_stop < 0) s_stop = s - 1;  // the row's last chunk (s was advanced past it)
       failed = true;
       break;
     }
@@ -265,11 +272,15 @@ __global__ void __launch_bounds__(MAXT, MINB) flow_forward_kernel(FlowArgs a) {
     }
   }
   if (failed) {
-    // the stage issued after the one that timed out may still be landing
-    if (BULK) {
-      (void)mbar_wait_bounded(&bars[0], 0u, 1u << 12);
-      (void)mbar_wait_bounded(&bars[1], 0u, 1u << 12);
+    // the stage whose wait ran out and the one issued after it may still be
+    // landing: each is the only phase of its barrier not yet observed, so
+    // its parity identifies it.  Thread 0 (the issuer) waits for both
+    // before the block, and its shared memory, goes away.
+    if (BULK && tid == 0 && s_stop >= 0) {
+      (void)mbar_wait_bounded(&bars[s_stop & 1], (s_stop >> 1) & 1, kDrainLimit);
+      if (s_stop + 1 < nstage) (void)mbar_wait_bounded(&bars[(s_stop + 1) & 1], ((s_stop + 1) >> 1) & 1, kDrainLimit);
     }
+    if (!BULK) cp_async_wait<0>();
     return;
   }
 #pragma unroll
@@ -436,6 +447,7 @@ using namespace bpl;
 extern "C" int bpl_flow_forward(const float* f0, const float* f1, float* cv_u, float* cv_v, float* u_star,
                                 float* v_star, int B, int C, int H, int W, int sws, int offset_u, int offset_v,
                                 int block_u, int block_v, void* stream) {
+  BPL_TRACE("bpl_flow_forward");
   BPL_REQUIRE(f0 && f1 && cv_u && cv_v && u_star && v_star, "flow_forward: null pointer");
   BPL_REQUIRE(B >= 1 && C >= 1 && H >= 1 && W >= 1, "flow_forward: bad shape");
   BPL_REQUIRE(B <= 65535 && H <= 65535, "flow_forward: B and H must be <= 65535");
@@ -475,6 +487,7 @@ extern "C" int bpl_flow_backward_ws(const float* f0, const float* f1, const floa
                                     const float* in_grad_v, const float* u_star, const float* v_star, float* df0,
                                     float* df1, void* workspace, size_t workspace_bytes, int B, int C, int H, int W,
                                     int sws, void* stream) {
+  BPL_TRACE("bpl_flow_backward_ws");
   BPL_REQUIRE(f0 && f1 && in_grad_u && in_grad_v && u_star && v_star && df0 && df1 && workspace,
               "flow_backward: null pointer");
   BPL_REQUIRE(B >= 1 && C >= 1 && H >= 1 && W >= 1 && sws >= 0, "flow_backward: bad shape");
@@ -504,6 +517,7 @@ extern "C" int bpl_flow_backward_ws(const float* f0, const float* f1, const floa
 extern "C" int bpl_flow_backward(const float* f0, const float* f1, const float* in_grad_u, const float* in_grad_v,
                                  const float* u_star, const float* v_star, float* df0, float* df1, int B, int C,
                                  int H, int W, int sws, void* stream) {
+  BPL_TRACE("bpl_flow_backward");
   BPL_REQUIRE(B >= 1 && C >= 1 && H >= 1 && W >= 1 && sws >= 0, "flow_backward: bad shape");
   cudaStream_t st = as_stream(stream);
   const size_t ws = bpl_flow_backward_workspace_size(B, C, H, W);

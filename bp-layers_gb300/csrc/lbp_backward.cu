@@ -155,6 +155,7 @@ extern "C" int bpl_lbp_backward(int variant, const float* jump, const float* edg
                                 const float* scale, float* grad_cost, float* grad_jump, float* grad_edge,
                                 void* workspace, size_t workspace_bytes, int B, int H, int W, int L,
                                 int Lv, int jump_batch, int edge_batch, void* stream) {
+  BPL_TRACE("bpl_lbp_backward");
   return lbp_backward_impl(0, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
                            stream);
@@ -165,6 +166,7 @@ extern "C" int bpl_lbp_backward_exact(int variant, const float* jump, const floa
                                       const float* scale, float* grad_cost, float* grad_jump, float* grad_edge,
                                       float* grad_messages, void* workspace, size_t workspace_bytes, int B, int H,
                                       int W, int L, int Lv, int jump_batch, int edge_batch, void* stream) {
+  BPL_TRACE("bpl_lbp_backward_exact");
   BPL_REQUIRE(grad_messages, "lbp_backward_exact: null grad_messages");
   return lbp_backward_impl(0, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
@@ -177,6 +179,7 @@ extern "C" int bpl_lbp_backward_passes(int variant, const float* jump, const flo
                                        const float* scale, float* grad_cost, float* grad_jump, float* grad_edge,
                                        void* workspace, size_t workspace_bytes, int B, int H, int W, int L, int Lv,
                                        int jump_batch, int edge_batch, int passes, void* stream) {
+  BPL_TRACE("bpl_lbp_backward_passes");
   BPL_REQUIRE(in_grad_batch_stride >= 0 && in_grad_slot_stride >= 0, "lbp_backward_passes: negative stride");
   return lbp_backward_impl(0, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
@@ -190,6 +193,7 @@ extern "C" int bpl_lbp_backward_passes_f16(int variant, const float* jump, const
                                            float* grad_edge, void* workspace, size_t workspace_bytes, int B, int H,
                                            int W, int L, int Lv, int jump_batch, int edge_batch, int passes,
                                            void* stream) {
+  BPL_TRACE("bpl_lbp_backward_passes_f16");
   BPL_REQUIRE(in_grad_batch_stride >= 0 && in_grad_slot_stride >= 0, "lbp_backward_passes: negative stride");
   return lbp_backward_impl(1, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
@@ -201,6 +205,7 @@ extern "C" int bpl_lbp_backward_f16(int variant, const float* jump, const float*
                                     float* grad_cost, float* grad_jump, float* grad_edge, void* workspace,
                                     size_t workspace_bytes, int B, int H, int W, int L, int Lv, int jump_batch,
                                     int edge_batch, void* stream) {
+  BPL_TRACE("bpl_lbp_backward_f16");
   return lbp_backward_impl(1, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
                            stream);

@@ -526,6 +526,7 @@ int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
   BwdArgs a = a0;
   const int per_warp = bwd::warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, V, sizeof(T)) * 4;
   for (int phase = 0; phase < 2; ++phase) {
+    BPL_TRACE(phase == 0 ? "lbp_backward: horizontal sweeps" : "lbp_backward: vertical sweeps");
     auto kern = (phase == 0) ? lbp_backward_kernel<K, V, LV, false, T> : lbp_backward_kernel<K, V, LV, true, T>;
     const int wmax = (phase == 0) ? bwd_warps_per_block<false, K>() : bwd_warps_per_block<true, K>();
     const int wpb = std::max(1, std::min(wmax, (200 * 1024) / per_warp));

@@ -10,8 +10,13 @@
 // inputs and outputs; only the scratch moves into the library.
 //
 // Costs and limits:
-//   * every GPU that loads the library holds kNoAllocScratchBytes of device
-//     memory for this array until the process exits;
+//   * every GPU on which the library's module is loaded holds
+//     kNoAllocScratchBytes of device memory for this array until the process
+//     exits.  With CUDA's lazy module loading (the default) the module, and
+//     with it the array, is loaded on a device by the library's first use
+//     there, which may be this entry point's first call: that call may then
+//     allocate the array and synchronise.  Hosts that need every call to be
+//     allocation-free make one warm-up call per device at start-up;
 //   * problems whose scratch (B*2*H*W*L floats) exceeds that size are
 //     rejected with BPL_ERR_INVALID_ARG;
 //   * all calls share the one array per device, so calls whose work overlaps
@@ -22,8 +27,10 @@
 //     including the zero rows at the image border, before the horizontal
 //     sweeps read them), so contents left by a previous call are harmless;
 //   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress with that device current); make that first call
-//     before any stream capture.
+//     (cudaGetSymbolAddress with that device current) and caches it per
+//     device ordinal: only the device's primary context (the runtime API's
+//     context, which torch uses) is supported.  Make that first call before
+//     any stream capture.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -66,6 +73,7 @@ extern "C" int bpl_lbp_backward_noalloc(int variant, const float* jump, const fl
                                         const float* scale, float* grad_cost, float* grad_jump,
                                         float* grad_edge, int B, int H, int W, int L, int Lv, int jump_batch,
                                         int edge_batch, void* stream) {
+  BPL_TRACE("bpl_lbp_backward_noalloc");
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1 && L >= 1, "lbp_backward_noalloc: bad shape B=%d H=%d W=%d L=%d", B, H,
               W, L);
   const size_t need = bpl_lbp_backward_workspace_size(B, H, W, L);

@@ -3,6 +3,7 @@
 
 namespace bpl {
 __device__ int g_bpl_error = 0;
+__device__ unsigned g_bpl_wait_limit = kWaitLimit;
 __device__ __align__(16) float g_zero_pairwise[96 * 96];
 }  // namespace bpl
 
@@ -90,6 +91,7 @@ extern "C" int bpl_lbp_forward(int variant, const float* cost, const float* jump
                                float* messages, void* argmin, int argmin_kind, float* scale, int B,
                                int H, int W, int L, int Lv, int jump_batch, int edge_batch, int delta,
                                void* stream) {
+  BPL_TRACE("bpl_lbp_forward");
   return lbp_forward_impl(0, variant, cost, jump, edge, messages, argmin, argmin_kind, scale, B, H, W, L, Lv,
                           jump_batch, edge_batch, delta, stream);
 }
@@ -98,6 +100,7 @@ extern "C" int bpl_lbp_forward_f16(int variant, const void* cost, const void* ju
                                    void* messages, void* argmin, int argmin_kind, float* scale, int B, int H,
                                    int W, int L, int Lv, int jump_batch, int edge_batch, int delta,
                                    void* stream) {
+  BPL_TRACE("bpl_lbp_forward_f16");
   return lbp_forward_impl(1, variant, cost, jump, edge, messages, argmin, argmin_kind, scale, B, H, W, L, Lv,
                           jump_batch, edge_batch, delta, stream);
 }

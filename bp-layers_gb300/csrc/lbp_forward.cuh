@@ -15,9 +15,12 @@
 //     and a second runs DOWN+UP for all columns: 2 launches per pass instead
 //     of 2(W-1)+2(H-1).
 //   * The per-pixel inputs that do not depend on the chain (cost and the two
-//     cross-direction messages) are streamed into a per-warp shared-memory
-//     ring NS pixels ahead with TMA 1-D bulk copies (cp.async.bulk +
-//     mbarrier), or 4-byte cp.async when a row is not 16-byte sized.
+//     cross-direction messages) are prefetched into registers one step ahead
+//     (coalesced loads of slots the running phase does not write).  The
+//     pixel-pairwise variant, whose step also needs an L x L matrix, streams
+//     them instead through a per-warp shared-memory ring NS pixels ahead with
+//     TMA 1-D bulk copies (cp.async.bulk + mbarrier, bounded waits), or
+//     4-byte cp.async when a row is not 16-byte sized.
 //   * Labels are spread over lanes (label = lane + 32k).  min/argmin and the
 //     exp-sum reproduce the reference's reduction tree (bpl_device.cuh); the
 //     exp/log of the normalisation are correctly rounded float evaluations
@@ -221,10 +224,10 @@ __device__ __forceinline__ void issue_slot(const FwdArgs& a, const Chain<T>& c, 
 // below nsteps: one mbarrier armed with the bytes of all of them.  With
 // cp.async rows (sps = 1) the caller commits one group per step.
 template <int VARIANT, typename T>
-__device__ __forceinline__ void issue_group(const FwdArgs& a, const Chain<T>& c, const WarpSmem& sm, int lroww,
+__device__ __forceinline__ bool issue_group(const FwdArgs& a, const Chain<T>& c, const WarpSmem& sm, int lroww,
                                             int i0, int g, int nsteps, int lane) {
   const int n = min(a.sps, nsteps - i0);
-  if (n <= 0) return;
+  if (n <= 0) return false;  // nothing to stage: the group stays unarmed
   uint64_t* bar = &sm.bars[g];
   if (a.vec4 && lane == 0) {
     const uint32_t rb = static_cast<uint32_t>(c.cnt) * static_cast<uint32_t>(sizeof(T));
@@ -235,6 +238,7 @@ __device__ __forceinline__ void issue_group(const FwdArgs& a, const Chain<T>& c,
     mbar_arrive_expect_tx(bar, static_cast<uint32_t>(n) * (3u * rb + mb));
   }
   for (int k = 0; k < n; ++k) issue_slot<VARIANT, T>(a, c, sm, lroww, i0 + k, g * a.sps + k, bar, lane);
+  return true;
 }
 
 // Stereo taps + edge weight for the 32 pixels of block b: lane j loads the
@@ -479,9 +483,11 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
     fence_mbar_init();
   }
   __syncwarp();
+  // ring groups with copies in flight (bit g), for the drain of a failed wait
+  uint32_t armed = 0u;
   if (kRing) {
     for (int i0 = 0; i0 < a.ns; i0 += G) {
-      issue_group<VARIANT, T>(a, c, sm, lroww, i0, i0 / G, nsteps, lane);
+      if (issue_group<VARIANT, T>(a, c, sm, lroww, i0, i0 / G, nsteps, lane)) armed |= 1u << (i0 / G);
       if (!a.vec4) cp_async_commit();
     }
   }
@@ -523,7 +529,12 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
     if (kRing && st == grp * G) {
       if (a.vec4) {
         ok = mbar_wait_bounded(&sm.bars[grp], (par >> grp) & 1u);
-        par ^= 1u << grp;
+        // a group whose wait ran out keeps its pending phase in `par` (and
+        // its bit in `armed`) for the drain below
+        if (ok) {
+          par ^= 1u << grp;
+          armed &= ~(1u << grp);
+        }
       } else {
         // groups 0..i have landed (one group per step, a.ns in flight)
         if (a.ns == 4) cp_async_wait<3>();
@@ -966,7 +977,8 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
 
     if (VARIANT == BPL_LBP_SEM_PIXEL) {
       __syncwarp();
-      if (st == grp * G + G - 1) issue_group<VARIANT, T>(a, c, sm, lroww, i + 1 - G + a.ns, grp, nsteps, lane);
+      if (st == grp * G + G - 1 && issue_group<VARIANT, T>(a, c, sm, lroww, i + 1 - G + a.ns, grp, nsteps, lane))
+        armed |= 1u << grp;
       if (!a.vec4) cp_async_commit();
     }
 
@@ -1037,9 +1049,11 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
 
   if (kRing && failed && a.vec4 && lane == 0) {
     // drain bulk copies still in flight before the warp's shared memory goes
-    // away: each group's pending phase is the one `par` expects next
-    // (bounded; a group with nothing in flight just runs out the bound)
-    for (int g = 0; g < a.ns / G; ++g) (void)mbar_wait_bounded(&sm.bars[g], (par >> g) & 1u, 1u << 12);
+    // away: each armed group's pending phase is the one `par` expects next
+    // (one phase per group at most is outstanding, so the parity is
+    // unambiguous)
+    for (int g = 0; g < a.ns / G; ++g)
+      if ((armed >> g) & 1u) (void)mbar_wait_bounded(&sm.bars[g], (par >> g) & 1u, kDrainLimit);
   }
   if (kRing && !a.vec4) cp_async_wait<0>();
 }
@@ -1101,6 +1115,7 @@ template <int K, int V, int KS, int NS, typename T>
 int launch_k(const FwdArgs& a0, cudaStream_t stream) {
   FwdArgs a = a0;
   for (int phase = 0; phase < 2; ++phase) {
+    BPL_TRACE(phase == 0 ? "lbp_forward: horizontal sweeps" : "lbp_forward: vertical sweeps");
     a.phase = phase;
     a.nchains = 2 * a.B * (phase == 0 ? a.H : a.W);
     int st;

@@ -81,6 +81,7 @@ using namespace bpl;
 
 extern "C" int bpl_upsample_add_beliefs(const float* beliefs, float* pv, int N, int h, int w, int d, float weight,
                                         void* stream) {
+  BPL_TRACE("bpl_upsample_add_beliefs");
   BPL_REQUIRE(beliefs && pv, "upsample_add_beliefs: null pointer");
   BPL_REQUIRE(N >= 1 && h >= 1 && w >= 1 && d >= 1, "upsample_add_beliefs: bad shape");
   const int64_t npx = static_cast<int64_t>(N) * 4 * h * w;  // fine pixels, one warp each

@@ -355,6 +355,7 @@ extern "C" int bpl_sad_volume_depth(int min_disp, int max_disp, float step) {
 
 extern "C" int bpl_sad_forward(const float* f0, const float* f1, float* out, int B, int C, int H, int W,
                                int min_disp, int max_disp, float step, void* stream) {
+  BPL_TRACE("bpl_sad_forward");
   BPL_REQUIRE(f0 && f1 && out, "sad_forward: null pointer");
   BPL_REQUIRE(B >= 1 && C >= 1 && H >= 1 && W >= 1, "sad_forward: bad shape");
   BPL_REQUIRE(step > 0.0f, "sad_forward: step must be > 0");
@@ -397,6 +398,7 @@ extern "C" int bpl_sad_forward(const float* f0, const float* f1, float* out, int
 extern "C" int bpl_sad_backward(const float* f0, const float* f1, const float* in_grad, float* df0, float* df1,
                                 int B, int C, int H, int W, int min_disp, int max_disp, int reference_channel_limit,
                                 void* stream) {
+  BPL_TRACE("bpl_sad_backward");
   BPL_REQUIRE(f0 && f1 && in_grad && df0 && df1, "sad_backward: null pointer");
   BPL_REQUIRE(B >= 1 && C >= 1 && H >= 1 && W >= 1 && max_disp >= min_disp, "sad_backward: bad shape");
   const int D = max_disp - min_disp + 1;

@@ -69,6 +69,18 @@ const char* bpl_last_error(void);
  * when no kernel reported an error. */
 int bpl_read_device_error(int* code);
 
+/* Sets the number of polls after which the kernels' bounded waits (the
+ * mbarrier waits of the TMA-staged pixel-pairwise LBP forward and of the flow
+ * SAD forward) give up, raise the device error word and return early with
+ * their outputs incomplete.  BPL_DEFAULT_WAIT_LIMIT (the value at load) is
+ * far beyond any copy's latency.  For tests of the timeout path: 0 makes
+ * every wait give up at once while the copies it waits for still land (a
+ * kernel whose wait gave up waits for its copies in flight before it exits).
+ * Applies to the current device.  No counterpart in the reference, whose
+ * kernels have no waits. */
+#define BPL_DEFAULT_WAIT_LIMIT 16777216u
+int bpl_set_wait_limit(unsigned polls);
+
 /*
  * Min-sum LBP forward: one pass of the four directional sweeps (RIGHT, LEFT,
  * DOWN, UP), messages updated in place.
@@ -339,7 +351,12 @@ int bpl_flow_backward_ws(const float* f0, const float* f1, const float* in_grad_
  * (BPL_ERR_INVALID_ARG otherwise).  All calls share that array: calls that
  * overlap on the GPU race and must be serialised by the caller.  The first
  * call on a device looks up the array's device address; make it before any
- * stream capture.
+ * stream capture.  With CUDA's lazy module loading (the default) the array
+ * comes into existence when the library's module is first loaded on a
+ * device, which this call may trigger: that first call may allocate and
+ * synchronise, so hosts that need every call allocation-free make one
+ * warm-up call per device at start-up.  Only the device's primary context
+ * (the runtime API's) is supported: the address is cached per device.
  */
 int bpl_lbp_backward_noalloc(int variant, const float* jump, const float* edge, const float* in_grad,
                              const float* messages, const void* argmin, int argmin_kind,

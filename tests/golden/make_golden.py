@@ -60,7 +60,20 @@ def _torch_paths():
     return inc, lib
 
 
-def build_reference(arch="103"):
+def _stamp(name, srcs):
+    h = hashlib.sha256()
+    for s in srcs:
+        with open(os.path.join(REF, s), "rb") as fh:
+            h.update(fh.read())
+    import torch
+    h.update(torch.__version__.encode())
+    return h.hexdigest()
+
+
+def build_reference(arch="103", names=None):
+    """Compiles the reference extensions `names` (default: all five) into
+    baseline/_ref/build/<name>.so; an extension whose sources and torch
+    version are unchanged since its last build is kept."""
     import torch
     inc, lib = _torch_paths()
     cuda_home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -68,7 +81,15 @@ def build_reference(arch="103"):
     abi = int(getattr(torch._C, "_GLIBCXX_USE_CXX11_ABI", 1))
     os.makedirs(BUILD, exist_ok=True)
     jobs = []
+    links = {}
     for name, srcs in EXTS.items():
+        if names is not None and name not in names:
+            continue
+        stamp = _stamp(name, srcs)
+        so = os.path.join(BUILD, name + ".so")
+        sp = os.path.join(BUILD, name + ".stamp")
+        if os.path.exists(so) and os.path.exists(sp) and open(sp).read() == stamp:
+            continue
         incs = ["-I" + os.path.join(REF, "include"), "-I" + py_inc] + ["-I" + p for p in inc]
         defs = [f"-DTORCH_EXTENSION_NAME={name}", "-DTORCH_API_INCLUDE_EXTENSION_H",
                 f"-D_GLIBCXX_USE_CXX11_ABI={abi}"]
@@ -91,7 +112,7 @@ def build_reference(arch="103"):
                ["-L" + p for p in lib] + ["-L" + os.path.join(cuda_home, "lib64")] + \
                ["-lc10", "-lc10_cuda", "-ltorch", "-ltorch_cpu", "-ltorch_cuda", "-ltorch_python", "-lcudart"] + \
                ["-Wl,-rpath," + p for p in lib] + ["-Wl,-rpath," + os.path.join(cuda_home, "lib64")]
-        EXTS[name] = (srcs, link)
+        links[name] = (link, stamp)
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -100,8 +121,10 @@ def build_reference(arch="103"):
 
     with ThreadPoolExecutor(max_workers=min(10, os.cpu_count() or 4)) as ex:
         list(ex.map(run, jobs))
-    for name, (_, link) in EXTS.items():
+    for name, (link, stamp) in links.items():
         run(link)
+        with open(os.path.join(BUILD, name + ".stamp"), "w") as fh:
+            fh.write(stamp)
 
 
 def load(name):

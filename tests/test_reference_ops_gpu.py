@@ -1,0 +1,458 @@
+"""Parity against the reference's own CUDA ops, at the benchmark sizes.
+
+The reference extensions are compiled on the GPU machine from the copy that
+tests/golden/prepare_reference.sh makes (baseline/_ref, git-ignored: it
+carries the one rename nvcc 13 needs, `namespace cuda` -> `namespace
+refcuda`), each under its own module name (make_golden.build_reference), so
+the three LBP variants load side by side.  The tests skip when that copy is
+absent.  Every case stays inside the reference kernels' valid range, checked
+by reading their index arithmetic: batch 1 per reference call (its forward,
+SAD and flow kernels process batch item 0 only), H <= W (its horizontal
+backward sizes a scratch buffer by W and indexes it by y), SAD step 1, flow
+windows of at most 108.
+
+Bars:
+* forward: argmin, messages and scales bit-identical to the reference op
+  (both evaluate the normalisation's exp/log to the same float: the
+  reference in double, this library in float-float with the reference's
+  double expression where the rounding is undecided);
+* backward: every element within atol + rtol*|ref| with rtol = 1e-4 and
+  atol = 1e-5 * max|ref| of the tensor (both sum with float atomics in an
+  order that changes from run to run, and this library applies the
+  normalisation's Jacobian as g - p*sum(g) instead of the reference's O(L^2)
+  loop, so results agree to rounding, and entries that cancel to near zero
+  carry an absolute error on the scale of the tensor);
+* SAD forward/backward and flow volumes, argmins and df0: bit-identical;
+  flow df1 (float atomics) within the backward tolerance.
+"""
+from __future__ import annotations
+
+import importlib.util
+import os
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF_ROOT = os.path.join(ROOT, "baseline", "_ref")
+REF_OPS = os.path.join(REF_ROOT, "ops")
+
+RTOL = 1e-4
+ATOL_REL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def ref():
+    if not os.path.isdir(REF_OPS):
+        pytest.skip("reference copy absent (run tests/golden/prepare_reference.sh <reference root>)")
+    import make_golden
+    make_golden.build_reference()
+    return {n: make_golden.load(n) for n in make_golden.EXTS}
+
+
+def dev():
+    return torch.device("cuda:0")
+
+
+def gen(seed):
+    return torch.Generator(device=dev()).manual_seed(seed)
+
+
+def assert_bits(a, b, what):
+    a, b = a.detach(), b.detach()
+    assert a.shape == b.shape, f"{what}: shape {tuple(a.shape)} vs {tuple(b.shape)}"
+    if a.dtype.is_floating_point:
+        ai = a.contiguous().view(torch.int32) if a.dtype == torch.float32 else a
+        bi = b.contiguous().view(torch.int32) if b.dtype == torch.float32 else b
+        bad = int((ai != bi).sum())
+    else:
+        bad = int((a != b).sum())
+    assert bad == 0, f"{what}: {bad} of {a.numel()} elements differ from the reference op"
+
+
+def assert_close(a, b, what, rtol=RTOL, atol_rel=ATOL_REL):
+    a, b = a.detach().float(), b.detach().float()
+    assert a.shape == b.shape, f"{what}: shape {tuple(a.shape)} vs {tuple(b.shape)}"
+    scale = float(b.abs().max())
+    d = (a - b).abs()
+    lim = atol_rel * scale + rtol * b.abs()
+    over = d > lim
+    if bool(over.any()):
+        i = int(torch.argmax((d - lim).flatten()))
+        pytest.fail(f"{what}: {int(over.sum())} of {b.numel()} elements outside atol+rtol*|ref| "
+                    f"(worst: got {float(a.flatten()[i])}, ref {float(b.flatten()[i])}, scale {scale})")
+
+
+def cost_volume(seed, B, H, W, L, std=2.0):
+    g = gen(seed)
+    s = std * torch.randn((B, H, W, L), device=dev(), generator=g)
+    return (-torch.softmax(s, dim=-1)).contiguous()
+
+
+def scalar_taps(B, H, W, L1=0.1, L2=0.5):
+    j = torch.zeros((B, 4, 6, H, W), device=dev())
+    j[:, :, 1] = L2
+    j[:, :, 2] = L1
+    j[:, :, 4] = L1
+    j[:, :, 5] = L2
+    return j.contiguous()
+
+
+def lognormal_edges(seed, B, H, W):
+    return torch.exp(0.3 * torch.randn((B, 4, H, W), device=dev(), generator=gen(seed))).contiguous()
+
+
+# ---------------------------------------------------------------------------
+# stereo LBP op: forward and backward_minsum at the full-size configuration
+
+
+def _stereo_pass_pair(ref_mod, cost, jump, edge, delta, passes):
+    """Runs `passes` in-place passes through the reference op and through this
+    library's drop-in module; returns both sides' per-pass outputs."""
+    from bpl_gb300.compat import lbp_stereo as ours
+    B, H, W, L = cost.shape
+    mr = torch.zeros((B, 4, H, W, L), device=dev())
+    mo = torch.zeros_like(mr)
+    out = []
+    for p in range(passes):
+        mr, ar, sr = ref_mod.forward_minsum(cost, jump, edge, mr, delta)
+        mo, ao, so = ours.forward_minsum(cost, jump, edge, mo, delta)
+        torch.cuda.synchronize()
+        assert_bits(ao, ar, f"pass {p} argmin")
+        assert_bits(mo, mr, f"pass {p} messages")
+        assert_bits(so, sr, f"pass {p} scale")
+        out.append((ar, sr, ao, so))
+    return mr, mo, out
+
+
+def test_stereo_full_size_forward_backward_matches_reference_op(ref):
+    """376x1240x192, B=1, the benchmark's scene: two in-place passes bit-equal,
+    then backward_minsum of the second pass against the reference's."""
+    import bench
+    from bpl_gb300.compat import lbp_stereo as ours
+    H, W, L, delta = bench.H, bench.W, bench.L, bench.DELTA
+    prob, edge, _ = bench.synth_inputs(torch, dev(), 0)
+    cost = (-prob).contiguous()
+    jump = scalar_taps(1, H, W)
+    st = ref["ref_lbp_stereo"]
+    mr, mo, per = _stereo_pass_pair(st, cost, jump, edge, delta, 2)
+    ar, sr, ao, so = per[-1]
+    gin = torch.randn((1, 4, H, W, L), device=dev(), generator=gen(7))
+    gr = st.backward_minsum(cost, jump, edge, gin, mr, ar, sr)
+    go = ours.backward_minsum(cost, jump, edge, gin, mo, ao, so)
+    torch.cuda.synchronize()
+    for name, a, b in zip(("grad_cost", "grad_jump", "grad_edge"), go[:3], gr[:3]):
+        assert_close(a, b, f"c1 {name}")
+    assert_bits(go[3], gr[3], "c1 grad_messages")
+
+
+def test_stereo_batch4_gradients_match_reference_op_per_sample(ref):
+    """4x256x512x96, per-pixel edge weights U[0.5,2]: this library runs the
+    batch of 4 at once, the reference op one item at a time (its forward
+    processes item 0 only); gradients of the cost volume, edge weights and
+    the L1/L2 taps (summed as the layer folds them) against the reference's."""
+    from bpl_gb300 import ops
+    B, H, W, L, delta = 4, 256, 512, 96, 3
+    cost = cost_volume(11, B, H, W, L)
+    edge = (0.5 + 1.5 * torch.rand((B, 4, H, W), device=dev(), generator=gen(12))).contiguous()
+    jump = scalar_taps(1, H, W)
+    gin = torch.randn((B, 4, H, W, L), device=dev(), generator=gen(13))
+    m = torch.zeros((B, 4, H, W, L), device=dev())
+    m, am, sc = ops.lbp_forward(ops.LBP_STEREO, cost, jump, edge, m, delta)
+    gc, gj_sum, ge, _ = ops.lbp_backward(ops.LBP_STEREO, jump, edge, gin, m, am, sc)
+    # the batch's tap gradient with a broadcast jump is summed over items; per
+    # item it is recomputed with a B=1 call for the comparison
+    st = ref["ref_lbp_stereo"]
+    tot_l1 = tot_l2 = 0.0
+    for n in range(B):
+        c, e, g = cost[n:n + 1].contiguous(), edge[n:n + 1].contiguous(), gin[n:n + 1].contiguous()
+        mr = torch.zeros((1, 4, H, W, L), device=dev())
+        mr, ar, sr = st.forward_minsum(c, jump, e, mr, delta)
+        torch.cuda.synchronize()
+        assert_bits(am[n:n + 1], ar, f"item {n} argmin")
+        assert_bits(m[n:n + 1], mr, f"item {n} messages")
+        gcr, gjr, ger, _ = st.backward_minsum(c, jump, e, g, mr, ar, sr)
+        _, gjo, _, _ = ops.lbp_backward(ops.LBP_STEREO, jump, e, g, m[n:n + 1].contiguous(),
+                                        am[n:n + 1].contiguous(), sc[n:n + 1].contiguous())
+        torch.cuda.synchronize()
+        assert_close(gc[n:n + 1], gcr, f"item {n} grad_cost")
+        assert_close(ge[n:n + 1], ger, f"item {n} grad_edge")
+        assert_close(gjo, gjr, f"item {n} grad_jump")
+        # dL1 and dL2 as the layer folds the taps [off, L2, L1, 0, L1, L2]
+        l1r = float(gjr[:, :, 2].double().sum() + gjr[:, :, 4].double().sum())
+        l2r = float(gjr[:, :, 1].double().sum() + gjr[:, :, 5].double().sum())
+        l1o = float(gjo[:, :, 2].double().sum() + gjo[:, :, 4].double().sum())
+        l2o = float(gjo[:, :, 1].double().sum() + gjo[:, :, 5].double().sum())
+        assert abs(l1o - l1r) <= 1e-4 * abs(l1r) + 1e-6, f"item {n} dL1 {l1o} vs {l1r}"
+        assert abs(l2o - l2r) <= 1e-4 * abs(l2r) + 1e-6, f"item {n} dL2 {l2o} vs {l2r}"
+        tot_l1 += l1r
+        tot_l2 += l2r
+    b1 = float(gj_sum[:, :, 2].double().sum() + gj_sum[:, :, 4].double().sum())
+    b2 = float(gj_sum[:, :, 1].double().sum() + gj_sum[:, :, 5].double().sum())
+    assert abs(b1 - tot_l1) <= 1e-4 * abs(tot_l1) + 1e-6, f"batch dL1 {b1} vs {tot_l1}"
+    assert abs(b2 - tot_l2) <= 1e-4 * abs(tot_l2) + 1e-6, f"batch dL2 {b2} vs {tot_l2}"
+
+
+# ---------------------------------------------------------------------------
+# semantic variants at the semantic configuration's size (per item)
+
+
+def _semantic_inputs(seed, H, W, L):
+    g = gen(seed)
+    cost = cost_volume(seed, 1, H, W, L)
+    p = 0.2 + 1.3 * torch.rand((2, L, L), device=dev(), generator=g)
+    p = 0.5 * (p + p.transpose(1, 2))
+    p = p * (1 - torch.eye(L, device=dev()))
+    edge = lognormal_edges(seed + 1, 1, H, W)
+    return cost, p, edge
+
+
+def test_semantic_global_matches_reference_op(ref):
+    """512x1024, L=19, global pairwise P per axis + per-pixel edge weights,
+    two in-place passes and backward_minsum."""
+    from bpl_gb300.compat import lbp_semantic_pw as ours
+    H, W, L = 512, 1024, 19
+    cost, p, edge = _semantic_inputs(21, H, W, L)
+    jump = torch.stack([p[0], p[0].t(), p[1], p[1].t()]).unsqueeze(0).contiguous()
+    sg = ref["ref_lbp_sem_global"]
+    mr = torch.zeros((1, 4, H, W, L), device=dev())
+    mo = torch.zeros_like(mr)
+    for it in range(2):
+        mr, ar, sr = sg.forward_minsum(cost, jump, edge, mr, L)
+        mo, ao, so = ours.forward_minsum(cost, jump, edge, mo, L)
+        torch.cuda.synchronize()
+        assert_bits(ao, ar, f"pass {it} argmin")
+        assert_bits(mo, mr, f"pass {it} messages")
+        assert_bits(so, sr, f"pass {it} scale")
+    gin = torch.randn((1, 4, H, W, L), device=dev(), generator=gen(22))
+    gr = sg.backward_minsum(cost, jump, edge, gin, mr, ar, sr)
+    go = ours.backward_minsum(cost, jump, edge, gin, mo, ao, so)
+    torch.cuda.synchronize()
+    for name, a, b in zip(("grad_cost", "grad_jump", "grad_edge"), go[:3], gr[:3]):
+        assert_close(a, b, f"semantic global {name}")
+
+
+def test_semantic_pixel_matches_reference_op(ref):
+    """512x1024, L=19, per-pixel pairwise (P scaled by exp(N(0,0.3)) per pixel
+    and axis), materialised as the reference wrapper builds it (4,H,W,L,L)."""
+    from bpl_gb300.compat import lbp_semantic_pw_pixel as ours
+    H, W, L = 512, 1024, 19
+    cost, p, edge = _semantic_inputs(31, H, W, L)
+    sc = torch.exp(0.3 * torch.randn((2, H, W, 1, 1), device=dev(), generator=gen(32)))
+    planes = torch.stack([p[0] * sc[0], p[1] * sc[1]])  # (2,H,W,L,L): LR and UD matrices per pixel
+    jump = torch.zeros((4, H, W, L, L), device=dev())
+    jump[0] = planes[0]
+    jump[1, :, 1:] = planes[0, :, :-1].transpose(-1, -2)
+    jump[2] = planes[1]
+    jump[3, 1:] = planes[1, :-1].transpose(-1, -2)
+    jump = jump.contiguous()
+    del planes
+    sp = ref["ref_lbp_sem_pixel"]
+    mr = torch.zeros((1, 4, H, W, L), device=dev())
+    mo = torch.zeros_like(mr)
+    for it in range(2):
+        mr, ar, sr = sp.forward_minsum(cost, jump, edge, mr, L)
+        mo, ao, so = ours.forward_minsum(cost, jump, edge, mo, L)
+        torch.cuda.synchronize()
+        assert_bits(ao, ar, f"pass {it} argmin")
+        assert_bits(mo, mr, f"pass {it} messages")
+        assert_bits(so, sr, f"pass {it} scale")
+    gin = torch.randn((1, 4, H, W, L), device=dev(), generator=gen(33))
+    gr = sp.backward_minsum(cost, edge, gin, mr, ar, sr)
+    go = ours.backward_minsum(cost, edge, gin, mo, ao, so)
+    torch.cuda.synchronize()
+    assert_close(go[0], gr[0], "semantic pixel grad_cost")
+    assert_close(go[1], gr[1], "semantic pixel grad_jump")
+
+
+# ---------------------------------------------------------------------------
+# SAD and flow SAD
+
+
+def test_stereo_sad_full_size_matches_reference_op(ref):
+    """376x1240, C=64, disparities 0..191: volume and both feature gradients
+    bit-identical."""
+    from bpl_gb300.compat import stereo_sad as ours
+    sad = ref["ref_stereo_sad"]
+    g = gen(41)
+    f0 = torch.randn((1, 64, 376, 1240), device=dev(), generator=g)
+    f1 = torch.randn((1, 64, 376, 1240), device=dev(), generator=g)
+    vr = sad.forward(f0, f1, 0, 191, 1.0)
+    vo = ours.forward(f0, f1, 0, 191, 1.0)
+    torch.cuda.synchronize()
+    assert_bits(vo, vr, "SAD volume")
+    gin = torch.randn(tuple(vr.shape), device=dev(), generator=g)
+    dr = sad.backward(f0, f1, 0, 191, gin)
+    do = ours.backward(f0, f1, 0, 191, gin)
+    torch.cuda.synchronize()
+    assert_bits(do[0], dr[0], "SAD df0")
+    assert_bits(do[1], dr[1], "SAD df1")
+
+
+def test_flow_sad_matches_reference_op(ref):
+    """384x512, C=32, window +-32 (sws 64): volumes and argmins bit-identical,
+    df0 bit-identical, df1 within the atomics tolerance."""
+    from bpl_gb300.compat import flow_mp_sad as ours
+    fl = ref["ref_flow_mp_sad"]
+    g = gen(51)
+    f0 = torch.randn((1, 32, 384, 512), device=dev(), generator=g)
+    f1 = torch.randn((1, 32, 384, 512), device=dev(), generator=g)
+    r = fl.forward(f0, f1, 64, 0, 0, 0, 0)
+    o = ours.forward(f0, f1, 64, 0, 0, 0, 0)
+    torch.cuda.synchronize()
+    for nm, a, b in zip(("cv_u", "cv_v", "u_star", "v_star"), o, r):
+        assert_bits(a, b, f"flow {nm}")
+    gu = torch.randn(tuple(r[0].shape), device=dev(), generator=g)
+    gv = torch.randn(tuple(r[1].shape), device=dev(), generator=g)
+    dr = fl.backward(f0, f1, 64, gu, gv, r[2], r[3])
+    do = ours.backward(f0, f1, 64, gu, gv, o[2], o[3])
+    torch.cuda.synchronize()
+    assert_bits(do[0], dr[0], "flow df0")
+    assert_close(do[1], dr[1], "flow df1")
+
+
+# ---------------------------------------------------------------------------
+# The reference's own wrapper modules, unchanged, on top of this library
+
+
+def _load_wrapper(relpath, alias, op_name, op_module):
+    """Imports the reference's wrapper file under `alias` with `op_name`
+    resolving to `op_module` (and corenet to the reference's copy)."""
+    saved = sys.modules.get(op_name)
+    sys.modules[op_name] = op_module
+    sys.path.insert(0, REF_ROOT)
+    try:
+        spec = importlib.util.spec_from_file_location(alias, os.path.join(REF_OPS, relpath))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+    finally:
+        sys.path.remove(REF_ROOT)
+        if saved is None:
+            sys.modules.pop(op_name, None)
+        else:
+            sys.modules[op_name] = saved
+    return mod
+
+
+def _run_stereo_wrapper(mod, prob, edge, upstream, L, delta, iters):
+    mp = mod.MessagePassing(dev(), iters, L, delta)
+    with torch.no_grad():
+        mp._L1.fill_(0.1)
+        mp._L2.fill_(0.5)
+    p = prob.clone().requires_grad_(True)
+    e = edge.clone().requires_grad_(True)
+    B, H, W, _ = prob.shape
+    m0 = torch.zeros((B, 4, H, W, L), device=dev(), requires_grad=True)
+    beliefs, _ = mp(p, e, None, None, m0)
+    beliefs.backward(upstream)
+    torch.cuda.synchronize()
+    return {"beliefs": beliefs.detach(), "prob.grad": p.grad, "edge.grad": e.grad, "L1.grad": mp._L1.grad,
+            "L2.grad": mp._L2.grad, "T.grad": mp.softmin.T.grad}
+
+
+def test_reference_stereo_wrapper_runs_unchanged_on_this_library(ref):
+    """ops/lbp_stereo/message_passing_op_cuda.py (MessagePassing +
+    LBPMinSumFunction, unchanged) with `pytorch_cuda_lbp_op` resolving to the
+    reference op and to this library: 3 iterations forward and backward at
+    256x512x96; beliefs equal, gradients within the backward tolerance; and
+    this library's own layer (fused epilogue, one-launch adjoint) against
+    both."""
+    import pytorch_cuda_lbp_op as ours_op
+    from bpl_gb300.layers.stereo import MessagePassing
+    w_ref = _load_wrapper("lbp_stereo/message_passing_op_cuda.py", "ref_wrapper_refop", "pytorch_cuda_lbp_op",
+                          ref["ref_lbp_stereo"])
+    w_ours = _load_wrapper("lbp_stereo/message_passing_op_cuda.py", "ref_wrapper_ours", "pytorch_cuda_lbp_op",
+                           ours_op)
+    H, W, L, delta, iters = 256, 512, 96, 3, 3
+    prob = (-cost_volume(61, 1, H, W, L)).contiguous()
+    edge = (0.5 + 1.5 * torch.rand((1, 4, H, W), device=dev(), generator=gen(62))).contiguous()
+    up = torch.randn((1, H, W, L), device=dev(), generator=gen(63))
+    r = _run_stereo_wrapper(w_ref, prob, edge, up, L, delta, iters)
+    o = _run_stereo_wrapper(w_ours, prob, edge, up, L, delta, iters)
+    assert_bits(o["beliefs"], r["beliefs"], "wrapper beliefs")
+    for k in ("prob.grad", "edge.grad"):
+        assert_close(o[k], r[k], f"wrapper {k}")
+    for k in ("L1.grad", "L2.grad", "T.grad"):
+        a, b = float(o[k].sum()), float(r[k].sum())
+        assert abs(a - b) <= 1e-4 * abs(b) + 1e-6, f"wrapper {k}: {a} vs {b}"
+    # this library's layer against the reference wrapper on the reference op
+    mp = MessagePassing(dev(), iters, L, delta)
+    with torch.no_grad():
+        mp._L1.fill_(0.1)
+        mp._L2.fill_(0.5)
+    p = prob.clone().requires_grad_(True)
+    e = edge.clone().requires_grad_(True)
+    m0 = torch.zeros((1, 4, H, W, L), device=dev(), requires_grad=True)
+    beliefs, _ = mp(p, e, None, None, m0)
+    beliefs.backward(up)
+    torch.cuda.synchronize()
+    assert_close(beliefs, r["beliefs"], "layer beliefs", rtol=1e-5, atol_rel=1e-6)
+    assert_close(p.grad, r["prob.grad"], "layer prob.grad")
+    assert_close(e.grad, r["edge.grad"], "layer edge.grad")
+    for k, t in (("L1.grad", mp._L1.grad), ("L2.grad", mp._L2.grad)):
+        a, b = float(t.sum()), float(r[k].sum())
+        assert abs(a - b) <= 1e-4 * abs(b) + 1e-6, f"layer {k}: {a} vs {b}"
+
+
+def test_reference_semantic_wrapper_runs_unchanged_on_this_library(ref):
+    """ops/lbp_semantic_pw/message_passing_op_cuda.py unchanged on the
+    reference op and on this library: 2 iterations at 128x256, L=19."""
+    from bpl_gb300.compat import lbp_semantic_pw as ours_op
+    w_ref = _load_wrapper("lbp_semantic_pw/message_passing_op_cuda.py", "ref_sem_wrapper_refop",
+                          "pytorch_cuda_lbp_op", ref["ref_lbp_sem_global"])
+    w_ours = _load_wrapper("lbp_semantic_pw/message_passing_op_cuda.py", "ref_sem_wrapper_ours",
+                           "pytorch_cuda_lbp_op", ours_op)
+    H, W, L = 128, 256, 19
+    cost, p, edge = _semantic_inputs(71, H, W, L)
+    prob = (-cost).contiguous()
+    up = torch.randn((1, H, W, L), device=dev(), generator=gen(72))
+    res = []
+    for mod in (w_ref, w_ours):
+        mp = mod.MessagePassing(dev(), 2, L, L)
+        pv = prob.clone().requires_grad_(True)
+        jv = p.unsqueeze(0).clone().requires_grad_(True)
+        m0 = torch.zeros((1, 4, H, W, L), device=dev(), requires_grad=True)
+        b = mp(pv, edge, m0, jv)
+        b.backward(up)
+        torch.cuda.synchronize()
+        res.append((b.detach(), pv.grad, jv.grad))
+    (br, gpr, gjr), (bo, gpo, gjo) = res
+    assert_bits(bo, br, "semantic wrapper beliefs")
+    assert_close(gpo, gpr, "semantic wrapper prob.grad")
+    assert_close(gjo, gjr, "semantic wrapper jump.grad")
+
+
+def test_reference_sad_and_flow_wrappers_run_unchanged_on_this_library(ref):
+    """ops/sad/stereo_sad.py and ops/flow_mp_sad/flow_mp_sad.py unchanged on
+    the reference ops and on this library's drop-in modules."""
+    import pytorch_cuda_flow_mp_sad_op as ours_flow
+    import pytorch_cuda_stereo_sad_op as ours_sad
+    g = gen(81)
+    f0 = torch.randn((1, 32, 96, 160), device=dev(), generator=g)
+    f1 = torch.randn((1, 32, 96, 160), device=dev(), generator=g)
+    res = []
+    for tag, sad_mod in (("ref", ref["ref_stereo_sad"]), ("ours", ours_sad)):
+        w = _load_wrapper("sad/stereo_sad.py", f"ref_sad_wrapper_{tag}", "pytorch_cuda_stereo_sad_op", sad_mod)
+        a, b = f0.clone().requires_grad_(True), f1.clone().requires_grad_(True)
+        v = w.StereoMatchingSadFunction.apply(a, b, 0, 47, 1.0)
+        v.backward(torch.ones_like(v))
+        torch.cuda.synchronize()
+        res.append((v.detach(), a.grad, b.grad))
+    for nm, x, y in zip(("volume", "df0", "df1"), res[1], res[0]):
+        assert_bits(x, y, f"SAD wrapper {nm}")
+    res = []
+    for tag, flow_mod in (("ref", ref["ref_flow_mp_sad"]), ("ours", ours_flow)):
+        w = _load_wrapper("flow_mp_sad/flow_mp_sad.py", f"ref_flow_wrapper_{tag}", "pytorch_cuda_flow_mp_sad_op",
+                          flow_mod)
+        a, b = f0.clone().requires_grad_(True), f1.clone().requires_grad_(True)
+        cu, cv, us, vs = w.FlowMpSadFunction.apply(a, b, 16)
+        (cu.sum() + 2.0 * cv.sum()).backward()
+        torch.cuda.synchronize()
+        res.append((cu.detach(), cv.detach(), us, vs, a.grad, b.grad))
+    for nm, x, y in zip(("cv_u", "cv_v", "u_star", "v_star", "df0"), res[1][:5], res[0][:5]):
+        assert_bits(x, y, f"flow wrapper {nm}")
+    assert_close(res[1][5], res[0][5], "flow wrapper df1")

@@ -4,10 +4,11 @@ It serves hosts that cannot call cudaMalloc when they run the backward (device
 memory owned by another runtime's pool, a fixed start-up budget, or loops that
 must not synchronise on an allocation): its scratch is a fixed device array
 inside the library.  These tests call it through the C ABI and compare it
-with the workspace-taking entry point, bpl_lbp_backward, on two calls in a row
-(the second call finds the array holding the first call's data).  Both entry
-points accumulate with float atomics, so results agree to float rounding, not
-bit for bit.  This file is collected last on purpose.
+with the workspace-taking entry point, bpl_lbp_backward, on two calls in a row:
+a larger problem first, then a smaller one, so that the second call finds the
+array holding the first call's data at and beyond every offset it uses.  Both
+entry points accumulate with float atomics, so results agree to float
+rounding, not bit for bit.  This file is collected last on purpose.
 """
 import ctypes
 
@@ -34,9 +35,10 @@ def test_noalloc_backward_matches_workspace_backward_twice():
     from bpl_gb300 import _lib, ops
     dev = torch.device("cuda:0")
     lib = _lib.lib()
-    for call, seed in enumerate((5, 6)):
+    # the first call's scratch (2*2*48*80*96 floats, 5.6 MiB) covers the second's
+    shapes = ((5, (2, 48, 80, 96)), (6, (1, 24, 40, 64)))
+    for call, (seed, (B, H, W, L)) in enumerate(shapes):
         g = cases.rng(seed)
-        B, H, W, L = 1, 24, 40, 64
         cost = torch.from_numpy(cases.random_cost(g, B, H, W, L)).to(dev)
         jump = torch.from_numpy(cases.random_taps8(g, B, H, W, offset_scale=1.0)).to(dev)
         edge = torch.from_numpy(cases.edge_weights(g, B, H, W)).to(dev)
