@@ -293,6 +293,47 @@ def run_ours(args):
                 "lbp_forward_pass_ms": sum(f16) / n16, "lbp_backward_pass_ms": sum(bw16) / n16,
                 "bytes_per_update": {"forward": 11, "backward": 12}}
 
+    # ---- the same step with argmin recomputation (no stored indices) -------
+    recompute = None
+    if not args.no_recompute:
+        mpr = MessagePassing(dev, ITERS, L, DELTA, recompute_argmin=True)
+        with torch.no_grad():
+            mpr._L1.fill_(0.1)
+            mpr._L2.fill_(0.5)
+
+        def held_by_forward(model):
+            prob.grad = None
+            m0 = torch.zeros((1, 4, H, W, L), device=dev, requires_grad=True)
+            torch.cuda.synchronize()
+            before = torch.cuda.memory_allocated(dev)
+            b, _ = model(prob, edge, None, None, m0)
+            torch.cuda.synchronize()
+            held = torch.cuda.memory_allocated(dev) - before - b.numel() * 4
+            b.backward(upstream)
+            return held
+
+        held_rec, held_std = held_by_forward(mpr), held_by_forward(mp)
+        n_rec = max(2, args.steps // 3)
+        for _ in range(2):
+            prob.grad = None
+            b = mpr(prob, edge, None, None, torch.zeros((1, 4, H, W, L), device=dev, requires_grad=True))[0]
+            b.backward(upstream)
+        barrier()
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r0.record(stream)
+        for _ in range(n_rec):
+            prob.grad = None
+            b = mpr(prob, edge, None, None, torch.zeros((1, 4, H, W, L), device=dev, requires_grad=True))[0]
+            b.backward(upstream)
+        r1.record(stream)
+        barrier()
+        ms_rec = r0.elapsed_time(r1) / n_rec
+        recompute = {"ms_per_step": ms_rec, "value": updates_per_step() / (ms_rec / 1e3), "unit": UNIT,
+                     "vs_stored_step": ms_rec / (ms_max / args.steps),
+                     "bytes_held_by_forward": {"recompute": held_rec, "stored_indices": held_std,
+                                               "indices_alone": ITERS * 4 * H * W * L},
+                     "steps": n_rec}
+
     U = updates_per_step()
     value = replicas.whole_job_rate(U, args.steps, world, ms_max)
     e2e_value = replicas.whole_job_rate(U, args.steps, world, e2e_ms)
@@ -334,6 +375,7 @@ def run_ours(args):
         # epilogue (forward, backward), the initial messages' gradient
         "gpu_launches": args.steps * (ITERS * 2 + 2 + 2 + 1),
         "fp16": fp16,
+        "recompute_argmin": recompute,
         "clocks": clk.summary(),
     }
     if world == 1 and not args.no_serving:
@@ -374,8 +416,9 @@ def run_serving(args):
     served by the continuous-batching engine (free-HBM admission, resident
     volumes, captured graphs), against plain per-request launches of the
     same requests.  Plain capacity is measured first (requests back to
-    back); the stream is then offered at `serve_load` times that capacity
-    to both, in real time."""
+    back); the stream is then offered at each of `serve_loads` times that
+    capacity, to both, in real time.  Also the device time of each shape's
+    captured graph per batch size (the batched cost per request)."""
     import numpy as np
     import torch
     from bpl_gb300 import serving
@@ -401,26 +444,54 @@ def run_serving(args):
     t = time.perf_counter()
     serving.run_plain(make(np.zeros(n)), realtime=False)
     plain_rps = n / (time.perf_counter() - t)
-    rate = args.serve_load * plain_rps
-    arrivals = np.cumsum(g.exponential(1.0 / rate, size=n))
-    plain = serving.latency_stats(serving.run_plain(make(arrivals)))
     eng = serving.ServingEngine(shapes, C=SERVE_C, max_batch=4, hbm_fraction=0.5, weights=probs, device=dev)
     eng.warm_up()
-    served_reqs = eng.serve(make(arrivals))
-    served = serving.latency_stats(served_reqs)
+    # device time of each shape's graph per batch size
+    graphs = {}
+    for s, sets in eng.sets.items():
+        ss = sets[0]
+        row = {}
+        for b in range(1, ss.cap + 1):
+            gr = ss.graph(b)
+            a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(ss.stream):
+                gr.replay()
+                a.record(ss.stream)
+                for _ in range(3):
+                    gr.replay()
+                e.record(ss.stream)
+            ss.stream.synchronize()
+            ms = a.elapsed_time(e) / 3
+            row[f"b{b}"] = {"ms": ms, "ms_per_request": ms / b}
+        graphs[f"{s[0]}x{s[1]}x{s[2]}"] = row
+    sweep = {}
+    for load in args.serve_loads:
+        rate = load * plain_rps
+        arrivals = np.cumsum(g.exponential(1.0 / rate, size=n))
+        plain = serving.latency_stats(serving.run_plain(make(arrivals)))
+        served_reqs = eng.serve(make(arrivals))
+        served = serving.latency_stats(served_reqs)
+        ok = sum(r.status == serving.DONE for r in served_reqs)
+        sweep[f"{load:g}x"] = {
+            "offered_rate_rps": rate, "completed": ok,
+            "served": {"requests_per_s": served["requests_per_s"], "p50_ms": served["p50_ms"],
+                       "p99_ms": served["p99_ms"]},
+            "plain": {"requests_per_s": plain["requests_per_s"], "p50_ms": plain["p50_ms"], "p99_ms": plain["p99_ms"]},
+            "throughput_vs_plain": (served["requests_per_s"] / plain["requests_per_s"]
+                                    if served["requests_per_s"] and plain["requests_per_s"] else None)}
     torch.cuda.synchronize()
     plan = eng.plan
     eng = None
     torch.cuda.empty_cache()
+    top = sweep[f"{max(args.serve_loads):g}x"]
     return {
         "requests": n, "mix": [{"H": s[0], "W": s[1], "D": s[2], "p": w} for s, w in SERVE_MIX],
-        "pipeline": "SAD (C=64) + softmax + 3-iteration FP16-storage BP forward + disparity argmin",
-        "offered_rate_rps": rate, "offered_load_vs_plain_capacity": args.serve_load,
+        "pipeline": "SAD (C=64) + cost -softmax(-SAD) in FP16 storage + 3-iteration FP16-storage BP forward + "
+                    "disparity from the messages (argmin), each a library kernel",
         "plain_capacity_rps": plain_rps,
-        "served": {"requests_per_s": served["requests_per_s"], "p50_ms": served["p50_ms"], "p99_ms": served["p99_ms"]},
-        "plain": {"requests_per_s": plain["requests_per_s"], "p50_ms": plain["p50_ms"], "p99_ms": plain["p99_ms"]},
-        "throughput_vs_plain": (served["requests_per_s"] / plain["requests_per_s"]
-                                if served["requests_per_s"] and plain["requests_per_s"] else None),
+        "offered_load_vs_plain_capacity": max(args.serve_loads),
+        "served": top["served"], "plain": top["plain"], "throughput_vs_plain": top["throughput_vs_plain"],
+        "sweep": sweep, "graph_ms": graphs,
         "slot_plan": {f"{s[0]}x{s[1]}x{s[2]}": {"sets": v[0], "batch": v[1]} for s, v in plan.items()},
     }
 
@@ -822,6 +893,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp16", action="store_true", help="skip the FP16-storage leg")
+    ap.add_argument("--no-recompute", action="store_true", help="skip the argmin-recompute leg")
     ap.add_argument("--ncu-case", action="store_true", help="small case for ncu captures")
     ap.add_argument("--no-serving", action="store_true", help="skip the served-stream leg")
     ap.add_argument("--serving-only", action="store_true", help="run only the served-stream leg")
@@ -832,8 +904,8 @@ def main():
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip timing the reference's own CUDA op (built from baseline/_ref)")
     ap.add_argument("--serve-requests", type=int, default=40)
-    ap.add_argument("--serve-load", type=float, default=4.0,
-                    help="offered arrival rate as a multiple of the plain per-request capacity")
+    ap.add_argument("--serve-loads", type=float, nargs="+", default=[0.5, 1.0, 2.0, 4.0],
+                    help="offered arrival rates as multiples of the plain per-request capacity")
     args = ap.parse_args()
     if args.ncu_case:
         run_ncu_case(args)

@@ -41,6 +41,9 @@ SIGNATURES = {
     "bpl_broadcast_slots": [c_void_p] * 2 + [c_int, ctypes.c_int64, c_int, c_void_p],
     "bpl_upsample_add_beliefs": [c_void_p] * 2 + [c_int] * 4 + [ctypes.c_float, c_void_p],
     "bpl_flow_backward_ws": [c_void_p] * 9 + [ctypes.c_size_t] + [c_int] * 5 + [c_void_p],
+    "bpl_cost_from_sad": [c_void_p, c_void_p, c_int] + [c_int] * 5 + [c_float, c_void_p],
+    "bpl_messages_argmin": [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int] + [c_int] * 6 + [c_void_p],
+    "bpl_beliefs_infer": [c_void_p, c_int, c_int, c_void_p] + [c_int] * 4 + [c_void_p],
     "bpl_lbp_backward_noalloc": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 4 + [c_int] * 7 + [c_void_p],
 }
 _RESTYPE = {"bpl_status_string": ctypes.c_char_p, "bpl_last_error": ctypes.c_char_p,

@@ -18,6 +18,10 @@ import torch.nn.functional as F
 
 from .. import ops
 
+# message slots (ops/lbp_stereo/src/util.cuh:7): slot k holds the message
+# received from the neighbour on side k
+LEFT, RIGHT, UP, DOWN = 0, 1, 2, 3
+
 
 class TemperatureSoftmin(nn.Module):
     """softmin(x / T) along `dim` with a learnable temperature (corenet.py:106-113)."""
@@ -109,32 +113,16 @@ class LBPMinSumFunction(torch.autograd.Function):
     returns in_grad as the message gradient.  adjoint "exact": the
     derivative of the forward; each pass keeps a copy of its own output
     messages and returns the gradient with respect to its input messages,
-    so chained passes differentiate exactly.
-
-    recompute=True stores no argmin indices: the pass keeps a copy of its
-    input messages instead and its backward re-runs the pass on a copy of
-    them, each warp regenerating its scanline's indices into a scratch
-    buffer (bit-identical: the same kernel on the same inputs), before the
-    adjoint.  Trades one forward pass of work in backward for the index
-    tensor (L bytes per pixel and direction) of every pass."""
+    so chained passes differentiate exactly.  (Argmin recomputation is an
+    option of LBPMinSumLoop, which sees all passes of a call.)"""
 
     @staticmethod
-    def forward(ctx, cost, edge, messages, delta, affinities, offset, adjoint="reference", recompute=False):
+    def forward(ctx, cost, edge, messages, delta, affinities, offset, adjoint="reference"):
         taps = pack_affinities(affinities, offset)
         L = cost.shape[-1]
         am_dtype = torch.uint8 if L <= 256 else torch.int16
         ctx.adjoint = adjoint
-        ctx.recompute = recompute
-        ctx.delta = int(delta)
-        ctx.am_dtype = am_dtype
         ctx.leaf_messages = messages.is_leaf
-        if recompute:
-            m_in = messages.detach().clone()
-            messages, _, scale = ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta),
-                                                 argmin_dtype=None)
-            own = messages.clone() if adjoint == "exact" else messages
-            ctx.save_for_backward(cost, taps, edge, own, m_in, scale)
-            return messages
         messages, argmin, scale = ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta),
                                                   argmin_dtype=am_dtype)
         own = messages.clone() if adjoint == "exact" else messages
@@ -143,20 +131,13 @@ class LBPMinSumFunction(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, in_grad):
-        cost, taps, edge, messages, saved, scale = ctx.saved_tensors
-        if ctx.recompute:
-            # the pass again, on a copy of its input: its argmin indices
-            # (the messages and scales it writes equal the saved ones)
-            _, argmin, _ = ops.lbp_forward(ops.LBP_STEREO, cost.detach(), taps, edge, saved.clone(), ctx.delta,
-                                           argmin_dtype=ctx.am_dtype)
-        else:
-            argmin = saved
+        cost, taps, edge, messages, argmin, scale = ctx.saved_tensors
         gc, gtaps, ge, gm = ops.lbp_backward(ops.LBP_STEREO, taps, edge, in_grad.contiguous(), messages, argmin,
                                              scale, copy_grad_messages=False, mode=ctx.adjoint)
         g_aff, g_off = unpack_affinity_grad(gtaps)
         if ctx.leaf_messages and ctx.needs_input_grad[2]:
             gm = ops.leaf_message_grad(gm)
-        return gc, ge, gm, None, g_aff, g_off, None, None
+        return gc, ge, gm, None, g_aff, g_off, None
 
 
 class LBPMinSumFunctionF16(torch.autograd.Function):
@@ -171,68 +152,142 @@ class LBPMinSumFunctionF16(torch.autograd.Function):
         taps = pack_affinities(affinities, offset)
         L = cost.shape[-1]
         am_dtype = torch.uint8 if L <= 256 else torch.int16
-        messages_h, argmin, scale = ops.lbp_forward_f16(ops.LBP_STEREO, cost_h, taps, edge, messages_h, int(delta), L,
-                                                        argmin_dtype=am_dtype)
-        ctx.save_for_backward(taps, edge, messages_h, argmin, scale)
+        messages_h, argmin, _ = ops.lbp_forward_f16(ops.LBP_STEREO, cost_h, taps, edge, messages_h, int(delta), L,
+                                                    argmin_dtype=am_dtype)
+        ctx.save_for_backward(taps, edge, messages_h, argmin)
         ctx.L = L
         ctx.leaf_messages = messages_h.is_leaf
         return messages_h
 
     @staticmethod
     def backward(ctx, in_grad):
-        taps, edge, messages_h, argmin, scale = ctx.saved_tensors
+        taps, edge, messages_h, argmin = ctx.saved_tensors
         gc, gtaps, ge = ops.lbp_backward_f16(ops.LBP_STEREO, taps, edge, in_grad.contiguous(), messages_h, argmin,
-                                             scale, ctx.L)
+                                             None, ctx.L)
         g_aff, g_off = unpack_affinity_grad(gtaps)
         gm = ops.leaf_message_grad(in_grad) if ctx.leaf_messages and ctx.needs_input_grad[3] else in_grad
         return gc[..., :ctx.L], None, ge, gm, None, g_aff, g_off
 
 
 class LBPMinSumLoop(torch.autograd.Function):
-    """`iters` LBP passes run in place with the reference adjoint, as one
-    autograd node.  The reference's per-pass nodes
+    """`iters` LBP passes run in place, as one autograd node.
+
+    Reference adjoint: the reference's per-pass nodes
     (message_passing_op_cuda.py:161-168) each read the final, overwritten
     messages in backward and pass in_grad through as the message gradient,
     so their adjoints are independent of each other: here they run as one
     launch (bpl_lbp_backward_passes), which triples the scanlines of the
     latency-bound horizontal sweeps at 3 iterations.  Gradients equal the
     chained per-pass nodes'.  FP32 or FP16 storage (cost_h and messages
-    half with the padded label axis)."""
+    half with the padded label axis).
+
+    recompute=True stores no argmin indices.  The forward keeps only a copy
+    of the initial messages' vertical slots (UP, DOWN): a pass reads its
+    horizontal slots only where it has written them itself, except at the
+    image borders no pass writes (LEFT at x=0, RIGHT at x=W-1), which the
+    final messages still hold, so those two slots plus the final messages
+    determine every pass exactly.  The backward re-runs the passes from that
+    state, each warp regenerating its scanline's indices (bit-identical: the
+    same kernel on the same inputs), and runs each pass's adjoint as soon as
+    its indices exist.  Persistent memory: 2 slots of the initial messages
+    in their storage type for the whole call (FP32: 8 B per pixel and
+    label) instead of 4 argmin bytes per pixel and label per pass; the
+    backward does `iters` forward passes more.  adjoint="exact" (FP32) runs
+    the passes' exact adjoints in reverse from the re-run's outputs."""
 
     @staticmethod
-    def forward(ctx, cost, cost_h, edge, messages, delta, affinities, offset, iters):
+    def forward(ctx, cost, cost_h, edge, messages, delta, affinities, offset, iters, adjoint="reference",
+                recompute=False):
         taps = pack_affinities(affinities, offset)
         half = messages.dtype == torch.float16
         L = cost.shape[-1]
         B, _, H, W, Ls = messages.shape
         am_dtype = torch.uint8 if L <= 256 else torch.int16
+        ctx.L, ctx.half, ctx.iters, ctx.delta = L, half, iters, int(delta)
+        ctx.adjoint, ctx.recompute, ctx.am_dtype = adjoint, recompute, am_dtype
+        ctx.leaf_messages = messages.is_leaf
+        if recompute:
+            vert0 = messages[:, UP:DOWN + 1].detach().clone()
+            for _ in range(iters):
+                if half:
+                    ops.lbp_forward_f16(ops.LBP_STEREO, cost_h, taps, edge, messages, int(delta), L, argmin_dtype=None)
+                else:
+                    ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta), argmin_dtype=None)
+            ctx.save_for_backward(cost, cost_h, taps, edge, messages, vert0)
+            return messages
         argmins = torch.empty((iters, B, 4, H, W, Ls), dtype=am_dtype, device=cost.device)
-        scales = torch.empty((iters, B, 4, H, W), dtype=torch.float32, device=cost.device)
+        # FP16: no scales (the adjoint normalises from the final rows)
+        scales = None if half else torch.empty((iters, B, 4, H, W), dtype=torch.float32, device=cost.device)
         for k in range(iters):
             if half:
                 ops.lbp_forward_f16(ops.LBP_STEREO, cost_h, taps, edge, messages, int(delta), L,
-                                    argmin_dtype=am_dtype, argmin=argmins[k], scale=scales[k])
+                                    argmin_dtype=am_dtype, argmin=argmins[k])
             else:
                 ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta), argmin_dtype=am_dtype,
                                 argmin=argmins[k], scale=scales[k])
         ctx.save_for_backward(taps, edge, messages, argmins, scales)
-        ctx.L = L
-        ctx.half = half
-        ctx.leaf_messages = messages.is_leaf
         return messages
 
     @staticmethod
     def backward(ctx, in_grad):
-        taps, edge, messages, argmins, scales = ctx.saved_tensors
-        # in_grad as autograd hands it over: the beliefs' gradient expanded over
-        # the four slots is read in place (slot stride 0), not materialised
-        gc, gtaps, ge = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, in_grad, messages, argmins, scales,
-                                                L=ctx.L)
+        if ctx.recompute:
+            gc, gtaps, ge, gm = LBPMinSumLoop._recompute_backward(ctx, in_grad)
+        else:
+            taps, edge, messages, argmins, scales = ctx.saved_tensors
+            # in_grad as autograd hands it over: the beliefs' gradient expanded
+            # over the four slots is read in place (slot stride 0), not materialised
+            gc, gtaps, ge = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, in_grad, messages, argmins, scales,
+                                                    L=ctx.L)
+            gm = in_grad
         g_aff, g_off = unpack_affinity_grad(gtaps)
         if ctx.half:
             gc = gc[..., :ctx.L]
-        gm = ops.leaf_message_grad(in_grad) if ctx.leaf_messages and ctx.needs_input_grad[3] else in_grad
-        return gc, None, ge, gm, None, g_aff, g_off, None
+        if ctx.leaf_messages and ctx.needs_input_grad[3]:
+            gm = ops.leaf_message_grad(gm)
+        return gc, None, ge, gm, None, g_aff, g_off, None, None, None
+
+    @staticmethod
+    def _recompute_backward(ctx, in_grad):
+        cost, cost_h, taps, edge, messages, vert0 = ctx.saved_tensors
+        half, L, delta = ctx.half, ctx.L, ctx.delta
+        # the state before the first pass: the final messages with the
+        # initial vertical slots back (see the class docstring)
+        m = messages.detach().clone()
+        m[:, UP:DOWN + 1] = vert0
+        B, _, H, W, Ls = m.shape
+        am = torch.empty((B, 4, H, W, Ls), dtype=ctx.am_dtype, device=m.device)
+        sc = None if half else torch.empty((B, 4, H, W), device=m.device)
+        ws = torch.empty(ops.lbp_backward_workspace_bytes(B, H, W, Ls), dtype=torch.uint8, device=m.device)
+        gc = gtaps = ge = None
+
+        def acc(a, b):
+            return b if a is None else a.add_(b)
+        if ctx.adjoint == "exact":
+            # exact adjoints run in reverse and need every pass's own output:
+            # keep them for the backward's duration (transient)
+            outs = []
+            for _ in range(ctx.iters):
+                m, a_k, s_k = ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, m, delta, argmin_dtype=ctx.am_dtype)
+                outs.append((m.clone(), a_k, s_k))
+            g = in_grad.contiguous()
+            for own, a_k, s_k in reversed(outs):
+                c_k, t_k, e_k, g = ops.lbp_backward(ops.LBP_STEREO, taps, edge, g, own, a_k, s_k, workspace=ws,
+                                                    copy_grad_messages=False, mode="exact")
+                gc, gtaps, ge = acc(gc, c_k), acc(gtaps, t_k), acc(ge, e_k)
+            return gc, gtaps, ge, g
+        g_in = in_grad
+        for _ in range(ctx.iters):
+            if half:
+                ops.lbp_forward_f16(ops.LBP_STEREO, cost_h, taps, edge, m, delta, L, argmin=am)
+                c_k, t_k, e_k = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, g_in, messages, am.unsqueeze(0),
+                                                        None, L=L, workspace=ws)
+            else:
+                ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, m, delta, argmin_dtype=ctx.am_dtype, argmin=am,
+                                scale=sc)
+                c_k, t_k, e_k = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, g_in, messages, am.unsqueeze(0),
+                                                        sc.unsqueeze(0), L=L, workspace=ws)
+            gc, gtaps, ge = acc(gc, c_k), acc(gtaps, t_k), acc(ge, e_k)
+        return gc, gtaps, ge, in_grad
 
 
 class MessagePassing(nn.Module):
@@ -273,8 +328,6 @@ class MessagePassing(nn.Module):
             raise ValueError("adjoint must be reference or exact")
         if adjoint == "exact" and storage != "fp32":
             raise ValueError("the exact adjoint runs with fp32 storage")
-        if recompute_argmin and storage != "fp32":
-            raise ValueError("argmin recomputation runs with fp32 storage")
         self.adjoint = adjoint
         self.recompute_argmin = recompute_argmin
         self.mode = mode
@@ -312,15 +365,15 @@ class MessagePassing(nn.Module):
                     m[..., :C] = messages.detach()
                 messages = m.requires_grad_(True)
             messages = LBPMinSumLoop.apply(cost, cost_h, edge_weights, messages, self.delta, affinities, offset,
-                                           self.max_iter)
+                                           self.max_iter, "reference", self.recompute_argmin)
             return BeliefsSoftmin.apply(messages, cost, self.softmin.T), messages
-        if self.adjoint == "reference" and not self.recompute_argmin:
+        if self.adjoint == "reference" or self.recompute_argmin:
             messages = LBPMinSumLoop.apply(cost, None, edge_weights, messages, self.delta, affinities, offset,
-                                           self.max_iter)
+                                           self.max_iter, self.adjoint, self.recompute_argmin)
         else:
             for _ in range(self.max_iter):
                 messages = LBPMinSumFunction.apply(cost, edge_weights, messages, self.delta, affinities, offset,
-                                                   self.adjoint, self.recompute_argmin)
+                                                   self.adjoint)
         return BeliefsSoftmin.apply(messages, cost, self.softmin.T), messages
 
 
@@ -337,7 +390,8 @@ class Inference(nn.Module):
 
     def forward(self, beliefs):
         if self.mode == "wta":
-            return torch.argmax(beliefs, dim=3, keepdim=True)
+            # one kernel pass (ops.beliefs_infer), the first index on ties like torch.argmax
+            return ops.beliefs_infer(beliefs.detach().contiguous(), "wta")
         if self.mode == "expectation":
             bn = beliefs / beliefs.sum(dim=3, keepdim=True)
             labels = torch.arange(beliefs.shape[3], device=beliefs.device, dtype=torch.float32).view(1, 1, 1, -1)
@@ -351,7 +405,11 @@ class Inference(nn.Module):
     @staticmethod
     def compute_sub_expectation(beliefs, support=3):
         """+-support window around the argmax, renormalised expectation
-        (inference_op.py:53-97)."""
+        (inference_op.py:53-97).  Without a gradient to carry, one kernel pass
+        (ops.beliefs_infer); with one, the torch form below (its gradient
+        flows to the window's beliefs as in the reference)."""
+        if not (beliefs.requires_grad and torch.is_grad_enabled()) and support <= 15:
+            return ops.beliefs_infer(beliefs.contiguous(), "sub-exp", support)
         N, H, W, K = beliefs.shape
         disp = beliefs.argmax(dim=-1).unsqueeze(-1)
         win = torch.arange(-support, support + 1, device=beliefs.device) + disp

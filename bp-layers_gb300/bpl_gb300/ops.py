@@ -311,24 +311,37 @@ def to_half_padded(t: torch.Tensor, L: int) -> torch.Tensor:
     return out
 
 
-def normalised_f16_messages(messages_h: torch.Tensor, scale: torch.Tensor, L: int) -> torch.Tensor:
+def normalised_f16_messages(messages_h: torch.Tensor, L: int, scale: torch.Tensor | None = None) -> torch.Tensor:
     """(B,4,H,W,L) float log-normalised messages (the reference's form) from
-    the min-referenced half rows and the scale of lbp_forward_f16.  Rows no
-    sweep wrote (scale 0: the first sender of each scanline) are returned
-    as stored."""
-    shift = torch.where(scale > 0, torch.log(scale), torch.zeros_like(scale))
-    return messages_h[..., :L].float() - shift.unsqueeze(-1)
+    the min-referenced half rows of lbp_forward_f16: row - log(sum(exp(row)))
+    over the L labels (or row - log(scale) with the scale lbp_forward_f16
+    returned).  Rows no sweep writes (slot LEFT at x=0, RIGHT at x=W-1, UP at
+    y=0, DOWN at y=H-1) are returned as stored."""
+    m = messages_h[..., :L].float()
+    if scale is not None:
+        shift = torch.where(scale > 0, torch.log(scale), torch.zeros_like(scale)).unsqueeze(-1)
+        return m - shift
+    out = m - torch.logsumexp(m, dim=-1, keepdim=True)
+    out[:, 0, :, 0] = m[:, 0, :, 0]
+    out[:, 1, :, -1] = m[:, 1, :, -1]
+    out[:, 2, 0] = m[:, 2, 0]
+    out[:, 3, -1] = m[:, 3, -1]
+    return out
 
 
 def lbp_forward_f16(variant: int, cost_h: torch.Tensor, jump: torch.Tensor, edge: torch.Tensor,
-                    messages_h: torch.Tensor, delta: int, L: int, argmin_dtype=torch.uint8, argmin=None, scale=None):
+                    messages_h: torch.Tensor, delta: int, L: int, argmin_dtype=torch.uint8, argmin=None, scale=None,
+                    want_scale: bool = False):
     """One LBP pass with FP16 storage.  cost_h (B,H,W,Lp) and messages_h
     (B,4,H,W,Lp) half with Lp = padded_labels(L); messages updated in place.
     The pixel variant takes jump (4,H,W,L,Lp) half, the stereo variant float
     taps.  Returns (messages_h, argmin (B,4,H,W,Lp), scale).  Message rows
-    are stored relative to the minimum of h, with scale the sum of exp of the
-    row: the reference's log-normalised message is row - log(scale)
-    (normalised_f16_messages)."""
+    are stored relative to the minimum of h (normalised_f16_messages gives
+    the reference's log-normalised form).  The per-message scale, the sum
+    of exp of the row, is computed only when asked for (a `scale` buffer or
+    want_scale=True; None is returned otherwise): the FP16 adjoint
+    recomputes the normalisation from the rows, and the stereo kernel's step
+    is shorter without it."""
     _check_input("cost_h", cost_h, dtype=torch.float16, dim=4)
     _check_input("messages_h", messages_h, dtype=torch.float16, dim=5)
     _check_input("edge", edge, dim=4)
@@ -350,8 +363,10 @@ def lbp_forward_f16(variant: int, cost_h: torch.Tensor, jump: torch.Tensor, edge
     kind = ARGMIN_NONE if argmin_dtype is None else _ARGMIN_KIND[argmin_dtype]
     if argmin is None and kind != ARGMIN_NONE:
         argmin = torch.zeros((B, 4, H, W, Lp), dtype=argmin_dtype, device=cost_h.device)
-    if scale is None:
+    if scale is None and want_scale:
         scale = torch.zeros((B, 4, H, W), dtype=torch.float32, device=cost_h.device)
+    if scale is not None:
+        _check_input("scale", scale, dim=4)
     st = _timed("lbp_forward_f16", lambda: lib().bpl_lbp_forward_f16(
         variant, _ptr(cost_h), _ptr(jump), _ptr(edge), _ptr(messages_h), _ptr(argmin), kind, _ptr(scale),
         B, H, W, L, Lv, jb, edge.shape[0], int(delta), _stream(cost_h)))
@@ -360,13 +375,14 @@ def lbp_forward_f16(variant: int, cost_h: torch.Tensor, jump: torch.Tensor, edge
 
 
 def lbp_backward_f16(variant: int, jump, edge: torch.Tensor, in_grad_h: torch.Tensor, messages_h: torch.Tensor,
-                     argmin: torch.Tensor, scale: torch.Tensor, L: int, workspace: torch.Tensor | None = None):
-    """Reference adjoint for FP16-stored messages (padded label axis).
+                     argmin: torch.Tensor, scale: torch.Tensor | None, L: int, workspace: torch.Tensor | None = None):
+    """Reference adjoint for FP16-stored messages (padded label axis).  The
+    normalisation's Jacobian is formed from the rows themselves (softmax of
+    the row), so `scale` is not needed (ignored; None allowed).
     Returns (grad_cost (B,H,W,Lp) float, grad_jump, grad_edge)."""
     _check_input("in_grad_h", in_grad_h, dtype=torch.float16, dim=5)
     _check_input("messages_h", messages_h, dtype=torch.float16, dim=5)
     _check_input("argmin", argmin, dtype=None, dim=5)
-    _check_input("scale", scale, dim=4)
     _check_input("edge", edge, dim=4)
     B, _, H, W, Lp = messages_h.shape
     if Lp != padded_labels(L):
@@ -404,7 +420,8 @@ def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.T
     pass order; in_grad and messages shared (the reference's backward of each
     pass reads the final messages and passes in_grad through).  FP32
     (messages float32) or FP16 storage (messages half, padded label axis,
-    L given).  Returns (grad_cost, grad_jump, grad_edge) summed over the
+    L given; scales may be None, the FP16 adjoint normalising from the
+    rows).  Returns (grad_cost, grad_jump, grad_edge) summed over the
     passes; the message gradient is in_grad."""
     half = messages.dtype == torch.float16
     if not isinstance(in_grad, torch.Tensor) or in_grad.dtype != messages.dtype or in_grad.dim() != 5 \
@@ -418,14 +435,20 @@ def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.T
     g_bstride, g_sstride = in_grad.stride(0), in_grad.stride(1)
     _check_input("messages", messages, dtype=None, dim=5)
     _check_input("argmins", argmins, dtype=None, dim=6)
-    _check_input("scales", scales, dim=5)
     _check_input("edge", edge, dim=4)
     B, _, H, W, Ls = messages.shape
     P = argmins.shape[0]
     if L is None:
         L = Ls
-    if tuple(argmins.shape) != (P, B, 4, H, W, Ls) or tuple(scales.shape) != (P, B, 4, H, W):
-        raise BplError("argmins/scales must be stacked (P,B,4,H,W,Ls) / (P,B,4,H,W)")
+    if tuple(argmins.shape) != (P, B, 4, H, W, Ls):
+        raise BplError("argmins must be stacked (P,B,4,H,W,Ls)")
+    if scales is None:
+        if not half:
+            raise BplError("scales are required with FP32 storage (the reference's backward_minsum argument)")
+    else:
+        _check_input("scales", scales, dim=5)
+        if tuple(scales.shape) != (P, B, 4, H, W):
+            raise BplError("scales must be stacked (P,B,4,H,W)")
     if half and Ls != padded_labels(L):
         raise BplError("FP16 messages must have the padded label axis")
     kind = _ARGMIN_KIND.get(argmins.dtype)
@@ -530,3 +553,63 @@ def beliefs_backward(messages: torch.Tensor, cost: torch.Tensor, temperature: to
         _ptr(grad_beliefs), _ptr(gz), _ptr(gT), B, H, W, L, Ls, _stream(beliefs)))
     check(st, "bpl_beliefs_backward")
     return gz, gT
+
+
+# ---------------------------------------------------------------------------
+# Epilogue kernels (cost from SAD, disparity from messages, inference)
+
+def cost_from_sad(sad: torch.Tensor, temperature: float = 1.0, half: bool = False,
+                  out: torch.Tensor | None = None) -> torch.Tensor:
+    """cost = -softmax(-sad / T) over the disparities of a (B,H,W,D) SAD
+    volume, one pass; half=True writes the FP16-storage layout (B,H,W,Lp)
+    with the label axis padded to a multiple of 8 (padding zeroed)."""
+    _check_input("sad", sad, dim=4)
+    B, H, W, D = sad.shape
+    Ls = padded_labels(D) if half else D
+    dtype = torch.float16 if half else torch.float32
+    if out is None:
+        out = torch.empty((B, H, W, Ls), dtype=dtype, device=sad.device)
+    elif out.dtype != dtype or tuple(out.shape) != (B, H, W, Ls) or not out.is_contiguous():
+        raise BplError(f"out must be a contiguous {(B, H, W, Ls)} {dtype} tensor")
+    st = _timed("cost_from_sad", lambda: lib().bpl_cost_from_sad(
+        _ptr(sad), _ptr(out), int(half), B, H, W, D, Ls, float(temperature), _stream(sad)))
+    check(st, "bpl_cost_from_sad")
+    return out
+
+
+def messages_argmin(messages: torch.Tensor, cost: torch.Tensor, L: int | None = None,
+                    out: torch.Tensor | None = None, out_dtype=torch.int64) -> torch.Tensor:
+    """(B,H,W) disparity = argmin over labels of ((((M0+M1)+M2)+M3)+cost),
+    first index: the beliefs' argmax without the belief volume.  messages
+    (B,4,H,W,Ls) and cost (B,H,W,Lc), each float or half (padded rows)."""
+    _check_input("messages", messages, dtype=None, dim=5)
+    _check_input("cost", cost, dtype=None, dim=4)
+    B, _, H, W, Ls = messages.shape
+    Lc = cost.shape[-1]
+    L = min(Ls, Lc) if L is None else int(L)
+    for nm, t in (("messages", messages), ("cost", cost)):
+        if t.dtype not in (torch.float32, torch.float16):
+            raise BplError(f"{nm} must be float32 or float16")
+    if out is None:
+        out = torch.empty((B, H, W), dtype=out_dtype, device=messages.device)
+    if out.dtype not in (torch.int64, torch.int32) or tuple(out.shape) != (B, H, W) or not out.is_contiguous():
+        raise BplError("out must be a contiguous (B,H,W) int64 or int32 tensor")
+    st = _timed("messages_argmin", lambda: lib().bpl_messages_argmin(
+        _ptr(messages), int(messages.dtype == torch.float16), _ptr(cost), int(cost.dtype == torch.float16),
+        _ptr(out), int(out.dtype == torch.int64), B, H, W, L, Ls, Lc, _stream(messages)))
+    check(st, "bpl_messages_argmin")
+    return out
+
+
+def beliefs_infer(beliefs: torch.Tensor, mode: str = "wta", support: int = 3) -> torch.Tensor:
+    """Inference on (B,H,W,L) beliefs: "wta" -> (B,H,W,1) int64 argmax,
+    "sub-exp" -> (B,H,W,1) float expectation over the argmax's window."""
+    _check_input("beliefs", beliefs, dim=4)
+    B, H, W, L = beliefs.shape
+    if mode not in ("wta", "sub-exp"):
+        raise BplError(f"beliefs_infer mode must be wta or sub-exp, got {mode!r}")
+    out = torch.empty((B, H, W, 1), dtype=torch.int64 if mode == "wta" else torch.float32, device=beliefs.device)
+    st = _timed("beliefs_infer", lambda: lib().bpl_beliefs_infer(
+        _ptr(beliefs), 0 if mode == "wta" else 1, int(support), _ptr(out), B, H, W, L, _stream(beliefs)))
+    check(st, "bpl_beliefs_infer")
+    return out

@@ -6,23 +6,39 @@ cost volume over D disparities, cost = -softmax(-SAD), a 3-iteration
 FP16-storage min-sum BP forward (truncated-linear pairwise L1/L2, unit edge
 weights), and the per-pixel argmin of the beliefs (the reference's stereo
 path: ops/sad/stereo_sad.py, ops/lbp_stereo/message_passing_op_cuda.py:138-177,
-inference_op.py:23-27).
+inference_op.py:23-27).  The pipeline is this library's kernels and one
+memset: SAD, the cost in FP16 storage (bpl_cost_from_sad), the BP passes,
+the disparity straight from the messages (bpl_messages_argmin).
 
 Design:
   * Admission by free-HBM budget: each (H,W,D) shape gets slot sets sized to
     a share of the free device memory at start-up; a waiting request is
-    admitted when a slot of its shape frees up.
+    admitted when a slot of its shape frees up.  A request of a shape without
+    slot sets gets one made for it while the budget and the device's free
+    memory allow, and is rejected (status "rejected") when they do not,
+    without stopping the stream.
   * Device-resident volumes: a slot set owns its feature, cost, message and
     output buffers for its lifetime; nothing is allocated per request.
   * Continuous batching: whenever a slot set is free, the requests of its
     shape that have arrived (up to its batch size) are launched as one
     batch, while other batches run; arrivals during a batch join the next.
-  * Captured graphs: each slot set replays one CUDA graph per batch size
-    (SAD, softmax, FP16 conversion, the BP passes, beliefs and argmin), on
+  * Captured graphs: each slot set replays one CUDA graph per batch size on
     its own stream, so batches of different shapes overlap on the device.
   * A batch of b requests runs the kernels with B = b: every request is
     computed exactly as it would be alone (the kernels treat batch items
     independently), so results do not depend on the mix.
+  * Failure handling on the host: cancel(rid) drops a waiting request or
+    discards a running one's result (status "cancelled"); a request with a
+    deadline that has not started when it passes is dropped (status
+    "expired"); a request that cannot get device memory is rejected
+    (status "rejected").  The kernels' device error word is read when a
+    batch completes; a batch whose kernels reported an error fails its
+    requests (status "failed").
+
+The scheduling (queues, admission, deadlines, cancellation, batching) is the
+host-only `Scheduler`, which drives any slot-set object with `cap`, `busy`,
+`launch(batch, use_graphs)` and `poll(now)`; `ServingEngine` runs it over GPU
+slot sets.
 """
 from __future__ import annotations
 
@@ -30,12 +46,16 @@ import collections
 import dataclasses
 import math
 import time
-from typing import Callable
+from typing import Callable, Iterable
 
 import torch
 
 from . import ops
 from .layers.stereo import pack_affinities
+
+# request states
+PENDING, WAITING, RUNNING, DONE = "pending", "waiting", "running", "done"
+CANCELLED, EXPIRED, REJECTED, FAILED = "cancelled", "expired", "rejected", "failed"
 
 
 @dataclasses.dataclass
@@ -45,8 +65,11 @@ class StereoRequest:
     f1: torch.Tensor
     D: int
     arrival: float = 0.0  # seconds after the start of the stream
+    deadline: float | None = None  # seconds after arrival by which it must have started (None: no limit)
     disparity: torch.Tensor | None = None  # (H,W) int64, device (filled in)
     t_done: float | None = None
+    status: str = PENDING
+    error: str | None = None
 
     @property
     def shape(self):
@@ -54,13 +77,11 @@ class StereoRequest:
 
 
 def slot_bytes(H: int, W: int, D: int, C: int) -> int:
-    """Device bytes one request of a slot set holds (buffers and the graph's
-    temporaries: SAD volume, softmax and belief volumes)."""
+    """Device bytes one request of a slot set holds: features, SAD volume
+    (float), cost and messages (half, padded labels), disparity."""
     Lp = ops.padded_labels(D)
     px = H * W
-    # features; SAD, cost, softmax and belief volumes (float); cost and
-    # messages (half); scales; disparity
-    return px * (2 * C * 4 + 4 * D * 4 + Lp * 2 + 4 * Lp * 2 + 4 * 4 + 8)
+    return px * (2 * C * 4 + 4 * D + 2 * Lp + 4 * Lp * 2 + 8)
 
 
 class SlotSet:
@@ -75,10 +96,8 @@ class SlotSet:
         self.f0 = torch.zeros((cap, C, H, W), device=device)
         self.f1 = torch.zeros((cap, C, H, W), device=device)
         self.sad = torch.zeros((cap, H, W, D), device=device)
-        self.cost = torch.zeros((cap, H, W, D), device=device)
         self.cost_h = torch.zeros((cap, H, W, Lp), dtype=torch.float16, device=device)
         self.msgs = torch.zeros((cap, 4, H, W, Lp), dtype=torch.float16, device=device)
-        self.scale = torch.zeros((cap, 4, H, W), device=device)
         self.disp = torch.zeros((cap, H, W), dtype=torch.int64, device=device)
         aff = torch.zeros((1, 4, 3, H, W), device=device)
         aff[:, :, :2] = L1
@@ -96,17 +115,12 @@ class SlotSet:
         D = self.D
         sad = self.sad[:b]
         ops.sad_forward(self.f0[:b], self.f1[:b], 0, D - 1, out=sad)
-        sad.neg_()
-        torch.neg(torch.softmax(sad, dim=-1), out=self.cost[:b])
-        self.cost_h[:b, ..., :D].copy_(self.cost[:b])
+        ops.cost_from_sad(sad, 1.0, half=True, out=self.cost_h[:b])
         self.msgs[:b].zero_()
         for _ in range(self.iters):
             ops.lbp_forward_f16(ops.LBP_STEREO, self.cost_h[:b], self.taps, self.edge, self.msgs[:b], self.delta, D,
-                                argmin_dtype=None, scale=self.scale[:b])
-        beliefs = self.cost[:b].clone()
-        for k in range(4):
-            beliefs.add_(self.msgs[:b, k, ..., :D])
-        torch.argmin(beliefs, dim=-1, out=self.disp[:b])
+                                argmin_dtype=None)
+        ops.messages_argmin(self.msgs[:b], self.cost_h[:b], D, out=self.disp[:b])
 
     def graph(self, b: int) -> torch.cuda.CUDAGraph:
         g = self.graphs.get(b)
@@ -146,12 +160,107 @@ class SlotSet:
         if not self.reqs or not self.event.query():
             return []
         done = self.reqs
+        # the kernels' bounded waits report through the device error word
+        # (the batch's event has completed, so reading it stalls nothing of
+        # this set; it synchronises the device)
+        code = ops.read_device_error()
         for i, r in enumerate(done):
-            with torch.cuda.stream(self.stream):
-                r.disparity = self.disp[i].clone()
+            if code:
+                r.status, r.error = FAILED, f"device error {code}"
+            elif r.status != CANCELLED:
+                with torch.cuda.stream(self.stream):
+                    r.disparity = self.disp[i].clone()
             r.t_done = now
         self.reqs = []
         return done
+
+
+class Scheduler:
+    """Host-side scheduling over slot sets (no device work of its own).
+
+    sets: {shape: [slot set, ...]}; make_set(shape) -> a new slot set for an
+    unplanned shape, raising MemoryError (or torch.cuda.OutOfMemoryError)
+    when the device cannot hold one; use_graphs is passed to launch()."""
+
+    def __init__(self, sets: dict, make_set: Callable | None = None, use_graphs: bool = True):
+        self.sets = {tuple(s): list(v) for s, v in sets.items()}
+        self.make_set = make_set
+        self.use_graphs = use_graphs
+        self.waiting: dict[tuple, collections.deque] = {s: collections.deque() for s in self.sets}
+        self.by_id: dict[int, StereoRequest] = {}
+        self.finished: list[StereoRequest] = []
+
+    # -- requests -------------------------------------------------------------
+    def submit(self, r: StereoRequest, now: float) -> bool:
+        """Queues an arrived request; False if it was rejected."""
+        self.by_id[r.rid] = r
+        s = r.shape
+        if s not in self.sets:
+            err = None
+            try:
+                if self.make_set is None:
+                    raise MemoryError("no slot set for this shape")
+                self.sets[s] = [self.make_set(s)]
+                self.waiting[s] = collections.deque()
+            except (MemoryError, torch.cuda.OutOfMemoryError) as exc:
+                err = f"out of device memory for shape {s}: {exc}"
+            if err is not None:
+                self._finish(r, REJECTED, now, err)
+                return False
+        r.status = WAITING
+        self.waiting[s].append(r)
+        return True
+
+    def cancel(self, rid: int, now: float = 0.0) -> bool:
+        """Cancels a waiting request (dropped) or a running one (its result
+        is discarded when its batch completes).  False if it already ended."""
+        r = self.by_id.get(rid)
+        if r is None or r.status not in (WAITING, RUNNING):
+            return False
+        if r.status == WAITING:
+            self.waiting[r.shape].remove(r)
+            self._finish(r, CANCELLED, now)
+        else:
+            r.status = CANCELLED  # its batch completes; the result is dropped then
+        return True
+
+    def _finish(self, r, status, now, err=None):
+        r.status, r.error, r.t_done = status, err, now
+        if status != DONE:
+            r.disparity = None
+        self.finished.append(r)
+
+    # -- progress -------------------------------------------------------------
+    @property
+    def active(self) -> bool:
+        return any(self.waiting.values()) or any(ss.busy for v in self.sets.values() for ss in v)
+
+    def step(self, now: float) -> bool:
+        """Collects completed batches, drops expired waiting requests and
+        launches batches on free slot sets.  Returns whether anything moved."""
+        moved = False
+        for sets in self.sets.values():
+            for ss in sets:
+                for r in ss.poll(now):
+                    moved = True
+                    if r.status in (CANCELLED, FAILED):
+                        self._finish(r, r.status, now, r.error)
+                    else:
+                        self._finish(r, DONE, now)
+        for s, q in self.waiting.items():
+            expired = [r for r in q if r.deadline is not None and now > r.arrival + r.deadline]
+            for r in expired:
+                q.remove(r)
+                self._finish(r, EXPIRED, now, "deadline passed before the request started")
+                moved = True
+            for ss in self.sets[s]:
+                if q and not ss.busy:
+                    batch = [q.popleft() for _ in range(min(ss.cap, len(q)))]
+                    for r in batch:
+                        r.status = RUNNING
+                    ss.launch(batch, use_graphs=self.use_graphs)
+                    moved = True
+        return moved
 
 
 class ServingEngine:
@@ -159,7 +268,7 @@ class ServingEngine:
 
     def __init__(self, shapes, C: int = 64, max_batch: int = 4, hbm_fraction: float = 0.5, weights=None,
                  iters: int = 3, L1: float = 0.1, L2: float = 0.5, delta: int = 3, device=None,
-                 budget_bytes: int | None = None, max_sets_per_shape: int = 2):
+                 budget_bytes: int | None = None, max_sets_per_shape: int = 2, new_shapes: bool = True):
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         shapes = [tuple(s) for s in shapes]
         weights = list(weights) if weights is not None else [1.0] * len(shapes)
@@ -167,13 +276,34 @@ class ServingEngine:
             free, _ = torch.cuda.mem_get_info(self.device)
             budget_bytes = int(free * hbm_fraction)
         self.budget = budget_bytes
+        self.C, self.iters, self.L1, self.L2, self.delta = C, iters, L1, L2, delta
         self.sets: dict[tuple, list[SlotSet]] = {s: [] for s in shapes}
         plan = plan_slot_sets(shapes, weights, C, max_batch, budget_bytes, max_sets_per_shape)
+        self.used = 0
         for s, (n_sets, cap) in plan.items():
             H, W, D = s
             for _ in range(n_sets):
                 self.sets[s].append(SlotSet(H, W, D, C, cap, iters, L1, L2, delta, self.device))
+                self.used += slot_bytes(H, W, D, C) * cap
         self.plan = plan
+        self.new_shapes = new_shapes
+        self.scheduler: Scheduler | None = None
+        self._now = lambda: 0.0
+
+    def _make_set(self, shape) -> SlotSet:
+        """One single-request slot set for a shape outside the plan, if it
+        fits the budget and the device's free memory."""
+        if not self.new_shapes:
+            raise MemoryError("the engine serves only its planned shapes")
+        H, W, D = shape
+        need = slot_bytes(H, W, D, self.C)
+        free, _ = torch.cuda.mem_get_info(self.device)
+        if self.used + need > self.budget or need > free:
+            raise MemoryError(f"needs {need} bytes, {max(0, self.budget - self.used)} left in the budget, "
+                              f"{free} free on the device")
+        ss = SlotSet(H, W, D, self.C, 1, self.iters, self.L1, self.L2, self.delta, self.device)
+        self.used += need
+        return ss
 
     def warm_up(self, use_graphs=True):
         """Captures every (slot set, batch size) graph before serving."""
@@ -184,41 +314,36 @@ class ServingEngine:
                         ss.graph(b)
         torch.cuda.synchronize(self.device)
 
-    def serve(self, requests: list[StereoRequest], use_graphs: bool = True, realtime: bool = True,
-              clock: Callable[[], float] = time.perf_counter) -> list[StereoRequest]:
-        """Serves the requests (sorted by arrival) and returns them completed."""
+    def cancel(self, rid: int) -> bool:
+        """Cancels a request of the stream being served (e.g. from on_tick)."""
+        return self.scheduler.cancel(rid, self._now()) if self.scheduler else False
+
+    def serve(self, requests: Iterable[StereoRequest], use_graphs: bool = True, realtime: bool = True,
+              clock: Callable[[], float] = time.perf_counter,
+              on_tick: Callable[["ServingEngine", float], None] | None = None) -> list[StereoRequest]:
+        """Serves the requests (by arrival time) and returns all of them
+        ended, each with its status.  on_tick(engine, now) is called on every
+        turn of the loop (e.g. to cancel requests)."""
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
-        waiting: dict[tuple, collections.deque] = {s: collections.deque() for s in self.sets}
-        for r in pending:
-            if r.shape not in self.sets:
-                raise ValueError(f"no slot set for shape {r.shape}")
-        done: list[StereoRequest] = []
+        sched = Scheduler(self.sets, self._make_set, use_graphs)
+        self.scheduler = sched
         t0 = clock()
-        while pending or any(waiting.values()) or any(ss.busy for v in self.sets.values() for ss in v):
+        self._now = lambda: clock() - t0
+        while pending or sched.active:
             now = clock() - t0
             while pending and (not realtime or pending[0].arrival <= now):
-                r = pending.popleft()
-                waiting[r.shape].append(r)
-            progressed = False
-            for sets in self.sets.values():
-                for ss in sets:
-                    fin = ss.poll(clock() - t0)
-                    if fin:
-                        done.extend(fin)
-                        progressed = True
-            for s, q in waiting.items():
-                for ss in self.sets[s]:
-                    if q and not ss.busy:
-                        batch = [q.popleft() for _ in range(min(ss.cap, len(q)))]
-                        ss.launch(batch, use_graphs=use_graphs)
-                        progressed = True
-            if not progressed:
-                if realtime and pending and not any(waiting.values()):
+                sched.submit(pending.popleft(), now)
+            if on_tick is not None:
+                on_tick(self, now)
+            if not sched.step(clock() - t0):
+                if realtime and pending and not any(sched.waiting.values()):
                     time.sleep(max(0.0, min(2e-4, pending[0].arrival - (clock() - t0))))
                 else:
-                    time.sleep(5e-5)
+                    time.sleep(2e-5)
         torch.cuda.synchronize(self.device)
-        return done
+        self.sets = sched.sets
+        self.scheduler = None
+        return sched.finished
 
 
 def plan_slot_sets(shapes, weights, C, max_batch, budget_bytes, max_sets_per_shape=2):
@@ -237,6 +362,7 @@ def plan_slot_sets(shapes, weights, C, max_batch, budget_bytes, max_sets_per_sha
         cap = int(max(1, min(max_batch, share // per[s])))
         n_sets = int(max(1, min(max_sets_per_shape, share // (per[s] * cap))))
         plan[s] = (n_sets, cap)
+
     # shrink until the plan fits (shares are floors; the minimum of one set
     # of one request per shape can exceed a small shape's share)
     def used(p):
@@ -270,20 +396,24 @@ def run_plain(requests: list[StereoRequest], iters=3, L1=0.1, L2=0.5, delta=3, r
         ss.stream.synchronize()
         r.disparity = ss.disp[0].clone()
         r.t_done = clock() - t0
+        r.status = DONE
         out.append(r)
     return out
 
 
 def latency_stats(reqs: list[StereoRequest]):
-    lat = sorted((r.t_done - r.arrival) * 1e3 for r in reqs)
+    """p50 / p99 latency (arrival to completion) and throughput of the
+    completed requests (status done, or never scheduled)."""
+    ok = [r for r in reqs if r.status in (DONE, PENDING) and r.t_done is not None]
+    lat = sorted((r.t_done - r.arrival) * 1e3 for r in ok)
     if not lat:
-        return {"p50_ms": None, "p99_ms": None}
+        return {"p50_ms": None, "p99_ms": None, "requests_per_s": None}
 
     def pct(p):
         k = min(len(lat) - 1, max(0, int(math.ceil(p / 100.0 * len(lat))) - 1))
         return lat[k]
-    span = max(r.t_done for r in reqs) - min(r.arrival for r in reqs)
-    return {"p50_ms": pct(50), "p99_ms": pct(99), "requests_per_s": len(reqs) / span if span > 0 else None}
+    span = max(r.t_done for r in ok) - min(r.arrival for r in ok)
+    return {"p50_ms": pct(50), "p99_ms": pct(99), "requests_per_s": len(ok) / span if span > 0 else None}
 
 
 def synth_request_features(H, W, D, C, seed, device):

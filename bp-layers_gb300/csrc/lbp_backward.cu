@@ -66,7 +66,9 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1, "lbp_backward: bad shape B=%d H=%d W=%d", B, H, W);
   BPL_REQUIRE(H <= 65535 && W <= 65535, "lbp_backward: H and W must be <= 65535");
   BPL_REQUIRE(L >= 1 && L <= 1024, "lbp_backward: L=%d outside [1, 1024]", L);
-  BPL_REQUIRE(edge && in_grad && messages && argmin && scale && grad_cost && grad_jump,
+  // the scale is part of the reference's signature (FP32 storage); FP16
+  // storage recomputes the normalisation from the rows and takes NULL
+  BPL_REQUIRE(edge && in_grad && messages && argmin && (scale || storage == 1) && grad_cost && grad_jump,
               "lbp_backward: null pointer");
   BPL_REQUIRE(variant == BPL_LBP_SEM_PIXEL || (jump && grad_edge), "lbp_backward: null jump/grad_edge");
   BPL_REQUIRE(argmin_kind >= BPL_ARGMIN_F32 && argmin_kind <= BPL_ARGMIN_U16, "lbp_backward: bad argmin kind");

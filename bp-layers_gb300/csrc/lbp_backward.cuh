@@ -213,7 +213,6 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
   const float* saved_dn = a.saved + (static_cast<int64_t>(v) * 2 + 1) * HWL;
   float* saved_out = a.saved + (static_cast<int64_t>(v) * 2 + (db == UP ? 0 : 1)) * HWL;
   float* gcost_n = a.grad_cost + static_cast<int64_t>(n) * HWL;
-  const float* scale_db = a.scale + (static_cast<int64_t>(v) * 4 + db) * HW;
   const float* edge_fd = a.edge + (static_cast<int64_t>(ne) * 4 + fd) * HW;
   const float* jump_fd = stereo ? a.jump + (static_cast<int64_t>(nj) * 4 + fd) * a.Lv * HW : nullptr;
   float* gjump_fd = stereo ? a.grad_jump + (static_cast<int64_t>(nj) * 4 + fd) * a.Lv * HW : nullptr;
@@ -269,17 +268,17 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
     }
   };
 
-  // per-step tile: stereo taps (Lv rows), edge weight (row Lv), scale (row Lv+1)
+  // per-step tile: stereo taps (Lv rows), edge weight (row Lv); row Lv+1 is
+  // unused (the normalisation's Jacobian needs no scale: see below)
   const int trow = a.Lv + 2;
   // Loaded 32 steps ahead and written to the tile when its block starts; the
   // registers are not read before then, so the loads never stall a step.
   // Constant register indices (a run-time index would put rg on the stack).
-  float ev = 0.0f, sv = 0.0f;
+  float ev = 0.0f;
   auto load_tile_regs = [&](int b, float (&rg)[16]) {
     const int k = min(32 * b + lane, nsteps - 1);  // lanes past the end reload the last step
     const int p = pin0 + k * dpin;
     ev = __ldg(edge_fd + p);
-    sv = __ldg(scale_db + p + dq);
     if (stereo) {
 #pragma unroll
       for (int j = 0; j < 16; ++j)
@@ -293,7 +292,6 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
         if (j < a.Lv) tile[j * 33 + lane] = rg[j];
     }
     tile[a.Lv * 33 + lane] = ev;
-    tile[(a.Lv + 1) * 33 + lane] = sv;
   };
 
   prefetch(0);
@@ -318,10 +316,9 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
     const float* tile = sm.tile + (b & 1) * (trow * 33);
 
     const float w = tile[a.Lv * 33 + j];
-    const float inv_s = (sizeof(T) == 4) ? 1.0f : __frcp_rn(tile[(a.Lv + 1) * 33 + j]);
     float g[K], pr[K];
     int am[K];
-    float sg = 0.0f, sa = 0.0f;
+    float sg = 0.0f, sa = 0.0f, se = 0.0f;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const bool valid = lvalid(kk);
@@ -330,10 +327,14 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
       // in the one accumulator (see the kernel's comment on the vertical
       // accumulators)
       g[kk] = valid ? (CROSS ? (bldf<T>(pg_[kk]) + pu_[kk]) + pd_[kk] : bldf<T>(pg_[kk])) : 0.0f;
-      // exp(m + log S) / S of the reference (:328-341) is exp(m) for a
-      // normalised message m = m_raw - log S; half rows hold m_raw - min h
-      // with their scale the sum of exp of the row, so exp(m) = exp(row) / scale
-      pr[kk] = valid ? __expf(bldf<T>(pm_[kk])) * inv_s : 0.0f;
+      // exp(m_raw) / S of the reference (:328-341), with m_raw rebuilt from
+      // the saved message plus log S, is exp(m) of the saved normalised
+      // message m: the messages' softmax over labels, whatever pass S came
+      // from.  Float rows are normalised (p = exp(m)); half rows hold
+      // m_raw - min h of the last pass, a constant away, so p = exp(row) /
+      // sum(exp(row)) with the sum taken here (se)
+      pr[kk] = valid ? __expf(bldf<T>(pm_[kk])) : 0.0f;
+      se += pr[kk];
       sg += g[kk];
       sa += accH[kk];
     }
@@ -349,6 +350,12 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
       for (int o2 = 8; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(FULL, v, o2);
       sg = __shfl_sync(FULL, v, 0);
       sa = __shfl_sync(FULL, v, 16);
+    }
+    if (sizeof(T) == 2) {
+      // p = exp(row) / se: scale the two sums instead of every p
+      const float inv_s = 1.0f / warp_sum(se);
+      sg *= inv_s;
+      sa *= inv_s;
     }
     float addH[K], addU[K], addD[K];
 #pragma unroll

@@ -24,7 +24,9 @@ int lbp_forward_impl(int storage, int variant, const void* cost, const void* jum
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1, "lbp_forward: bad shape B=%d H=%d W=%d", B, H, W);
   BPL_REQUIRE(H <= 65535 && W <= 65535, "lbp_forward: H and W must be <= 65535");
   BPL_REQUIRE(L >= 1 && L <= 1024, "lbp_forward: L=%d outside [1, 1024]", L);
-  BPL_REQUIRE(cost && jump && edge && messages && scale, "lbp_forward: null pointer");
+  // scale: required for FP32 storage (the reference's output), optional for
+  // FP16 storage (its adjoint recomputes the normalisation from the rows)
+  BPL_REQUIRE(cost && jump && edge && messages && (scale || storage == 1), "lbp_forward: null pointer");
   BPL_REQUIRE(delta >= 0 && delta <= 65535, "lbp_forward: delta=%d is not a uint16", delta);
   BPL_REQUIRE(edge_batch == 1 || edge_batch == B, "lbp_forward: edge batch %d must be 1 or B", edge_batch);
   BPL_REQUIRE(argmin_kind >= BPL_ARGMIN_NONE && argmin_kind <= BPL_ARGMIN_U16, "lbp_forward: bad argmin kind");

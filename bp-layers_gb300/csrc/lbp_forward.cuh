@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
   // labels copied per row: the warp's labels below Ls (padding included, so
   // half rows stay 16-byte sized)
   c.cnt = max(0, min(lroww, Ls - c.t0));
-  float* scale_out = a.scale + (static_cast<int64_t>(c.n) * 4 + od) * HW;
+  float* scale_out = a.scale ? a.scale + (static_cast<int64_t>(c.n) * 4 + od) * HW : nullptr;  // NULL: FP16, not asked for
   const float* gjump =
       (VARIANT == BPL_LBP_SEM_GLOBAL) ? static_cast<const float*>(a.jump) + static_cast<int64_t>(c.dir) * L * L : nullptr;
   const bool stereo = (VARIANT == BPL_LBP_STEREO);
@@ -1033,7 +1033,7 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
       }
     }
     // (float)max((double)sum, 1e-45): the smallest positive float when sum is 0
-    if (wic == 0 && lane == 0) scale_out[pq] = (sum > 0.0f) ? sum : __int_as_float(1);
+    if (wic == 0 && lane == 0 && scale_out) scale_out[pq] = (sum > 0.0f) ? sum : __int_as_float(1);
 
     // next tap block
     if (j == 31 || i == nsteps - 1) {

@@ -255,6 +255,46 @@ int bpl_broadcast_slots(const void* src, void* dst, int B, int64_t row_elems, in
 int bpl_upsample_add_beliefs(const float* beliefs, float* pv, int N, int h, int w, int d, float weight,
                              void* stream);
 
+/*
+ * Cost volume from a SAD volume (the reference's matching step,
+ * matching.py:22-25, followed by MessagePassing's cost = -prob,
+ * message_passing_op_cuda.py:162): cost[n,y,x,t] = -softmax_t(-sad[n,y,x,t] /
+ * temperature) over the D disparities, in one pass.  sad (B,H,W,D) float;
+ * cost (B,H,W,Ls) float (cost_half = 0) or half (1), labels D..Ls-1 of each
+ * row set to zero (Ls = D, or D rounded up to 8 for the FP16-storage
+ * layout).  exp by expf and the sum in any order: within float rounding of
+ * torch's softmax, not bit-identical to it.  No counterpart in the
+ * reference's ops (torch calls there).
+ */
+int bpl_cost_from_sad(const float* sad, void* cost, int cost_half, int B, int H, int W, int D, int Ls,
+                      float temperature, void* stream);
+
+/*
+ * Per-pixel disparity straight from the messages: disparity[n,y,x] =
+ * argmin_t ((((M0 + M1) + M2) + M3) + cost)[t], first index on ties: the
+ * label whose belief softmin(...) is largest (the reference's
+ * MessagePassing beliefs followed by Inference "wta",
+ * message_passing_op_cuda.py:170-173, inference_op.py:23-27), without the
+ * belief volume.  messages (B,4,H,W,Ls) float or half (messages_half); cost
+ * (B,H,W,Lc) float or half (cost_half); disparity (B,H,W) int32 or int64
+ * (disparity_int64).  No counterpart in the reference.
+ */
+int bpl_messages_argmin(const void* messages, int messages_half, const void* cost, int cost_half,
+                        void* disparity, int disparity_int64, int B, int H, int W, int L, int Ls, int Lc,
+                        void* stream);
+
+/*
+ * Inference on a belief volume (B,H,W,L) float (Inference.forward,
+ * ops/lbp_stereo/inference_op.py:22-97): mode 0 "wta", out (B,H,W) int64 =
+ * argmax over labels (first index, as torch.argmax); mode 1 "sub-exp", out
+ * (B,H,W) float = the expectation of the label over the argmax's
+ * +-support window, window labels clamped to [0, L-1], renormalised
+ * (compute_sub_expectation, :53-97; support <= 15).  One pass instead of
+ * the reference's gather and three reductions.
+ */
+int bpl_beliefs_infer(const float* beliefs, int mode, int support, void* out, int B, int H, int W, int L,
+                      void* stream);
+
 /* Disparity count D of the SAD volume: (int)((max_disp - min_disp + 1) / step)
  * (ops/sad/src/stereo_sad_kernel.cu:122); -1 for a non-positive step. */
 int bpl_sad_volume_depth(int min_disp, int max_disp, float step);

@@ -85,33 +85,56 @@ def test_message_passing_exact_adjoint_through_iterations():
     np.testing.assert_allclose(m0.grad.detach().cpu().numpy(), G, atol=2e-4 * max(1.0, np.abs(G).max()))
 
 
-@pytest.mark.parametrize("adjoint", ["reference", "exact"])
-def test_recompute_argmin_variant_matches_stored(adjoint):
-    """MessagePassing(recompute_argmin=True) stores no indices and
-    regenerates them per scanline in backward: gradients equal those of the
-    index-storing variant (config: B=4, per-pixel edge weights U[0.5,2],
-    reduced from 256x512x96 to keep the test short)."""
+@pytest.mark.parametrize("adjoint,storage,size", [("reference", "fp32", "full"), ("exact", "fp32", "small"),
+                                                  ("reference", "fp16", "small")])
+def test_recompute_argmin_variant_matches_stored(adjoint, storage, size):
+    """MessagePassing(recompute_argmin=True) stores no indices: its forward
+    keeps the initial vertical message slots only, its backward re-runs the
+    passes (regenerating every scanline's indices) and runs their adjoints.
+    Gradients equal those of the index-storing variant, and the memory the
+    forward leaves for the backward is below the stored indices.  Config:
+    B=4, 256x512x96, per-pixel edge weights U[0.5,2], 3 iterations (the
+    exact adjoint and FP16 storage on a 32x64 crop)."""
     from bpl_gb300.layers.stereo import MessagePassing
     dev = torch.device("cuda:0")
     g = cases.rng(23)
-    B, H, W, L, iters = 4, 32, 64, 96, 3
-    prob = torch.from_numpy(cases.softmax_np(g.normal(0, 2, size=(B, H, W, L)).astype(np.float32))).to(dev)
-    edge = torch.from_numpy(g.uniform(0.5, 2.0, size=(B, 4, H, W)).astype(np.float32)).to(dev)
-    up = torch.randn((B, H, W, L), device=dev, generator=torch.Generator(device=dev).manual_seed(2))
-    grads = []
+    B, H, W, L, iters = (4, 256, 512, 96, 3) if size == "full" else (4, 32, 64, 96, 3)
+    gen = torch.Generator(device=dev).manual_seed(2)
+    prob = torch.softmax(2.0 * torch.randn((B, H, W, L), device=dev, generator=gen), dim=-1)
+    edge = (0.5 + 1.5 * torch.rand((B, 4, H, W), device=dev, generator=gen)).contiguous()
+    up = torch.randn((B, H, W, L), device=dev, generator=gen)
+    grads, held = [], []
     for rec in (False, True):
-        mp = MessagePassing(dev, iters, L, 3, adjoint=adjoint, recompute_argmin=rec)
+        mp = MessagePassing(dev, iters, L, 3, storage=storage, adjoint=adjoint, recompute_argmin=rec)
         with torch.no_grad():
             mp._L1.fill_(0.1)
             mp._L2.fill_(0.5)
         p = prob.clone().requires_grad_(True)
         e = edge.clone().requires_grad_(True)
-        beliefs, _ = mp(p, e, None, None, torch.zeros((B, 4, H, W, L), device=dev, requires_grad=True))
+        m0 = None if storage == "fp16" else torch.zeros((B, 4, H, W, L), device=dev, requires_grad=True)
+        torch.cuda.synchronize()
+        before = torch.cuda.memory_allocated(dev)
+        beliefs, msgs = mp(p, e, None, None, m0)
+        torch.cuda.synchronize()
+        # what the forward leaves for the backward, beyond its outputs
+        held.append(torch.cuda.memory_allocated(dev) - before - beliefs.numel() * 4
+                    - (msgs.numel() * msgs.element_size() if m0 is None else 0))
         beliefs.backward(up)
         grads.append((beliefs.detach(), p.grad, e.grad, mp._L1.grad.item(), mp._L2.grad.item()))
+        del beliefs, msgs, m0
+    if adjoint == "reference":
+        argmin_bytes = iters * B * 4 * H * W * (ops_padded(L) if storage == "fp16" else L)
+        print(f"{storage} held by the forward: stored indices {held[0] / 2**20:.1f} MiB, "
+              f"recompute {held[1] / 2**20:.1f} MiB (indices alone {argmin_bytes / 2**20:.1f} MiB)")
+        assert held[1] < argmin_bytes <= held[0]
     (b0, gp0, ge0, l10, l20), (b1, gp1, ge1, l11, l21) = grads
     assert torch.equal(b0, b1)
     assert (gp0 - gp1).abs().max().item() <= 1e-5 * max(1.0, gp0.abs().max().item())
     assert (ge0 - ge1).abs().max().item() <= 1e-5 * max(1.0, ge0.abs().max().item())
     assert abs(l10 - l11) <= 1e-5 * max(1.0, abs(l10))
     assert abs(l20 - l21) <= 1e-5 * max(1.0, abs(l20))
+
+
+def ops_padded(L):
+    from bpl_gb300 import ops
+    return ops.padded_labels(L)
