@@ -647,7 +647,29 @@ def run_other_configs():
 
     out["semantic_pixel_2x512x1024x19"]["layer_pass_fwd_bwd_ms"] = {"materialised_packing": timed(packed_pass),
                                                                       "two_planes_in_kernels": timed(planes_pass)}
-    del cost, j4, m, am, sc, gin, ch, jh, mh, amh, sch, jp
+    del j4, ch, jh, mh, amh, sch, jp
+    # the semantic configuration's global form (lbp_semantic_pw): one 19x19
+    # matrix per axis (symmetric, zero diagonal, off-diagonal U[0.2,1.5]),
+    # per-pixel edge weights exp(N(0,0.3)), per pass
+    P = g.uniform(0.2, 1.5, size=(2, Ls, Ls)).astype(np.float32)
+    P = 0.5 * (P + P.transpose(0, 2, 1))
+    for k in range(2):
+        np.fill_diagonal(P[k], 0.0)
+    jg = torch.from_numpy(np.stack([P[0], P[0].T, P[1], P[1].T])[None].copy()).to(dev)
+    eg = torch.exp(0.3 * torch.randn((B, 4, Hs, Ws), device=dev))
+    fwd_g = timed(lambda: ops.lbp_forward(ops.LBP_SEM_GLOBAL, cost, jg, eg, m, Ls, argmin_dtype=torch.uint8,
+                                          argmin=am, scale=sc))
+    bwd_g = timed(lambda: ops.lbp_backward(ops.LBP_SEM_GLOBAL, jg, eg, gin, m, am, sc, copy_grad_messages=False))
+    ch = ops.to_half_padded(cost, Ls)
+    mh = torch.zeros((B, 4, Hs, Ws, ops.padded_labels(Ls)), dtype=torch.float16, device=dev)
+    fwd_g16 = timed(lambda: ops.lbp_forward_f16(ops.LBP_SEM_GLOBAL, ch, jg, eg, mh, Ls, Ls, argmin_dtype=torch.uint8))
+    out["semantic_global_2x512x1024x19"] = {
+        "fp32_forward_pass_ms": fwd_g, "fp32_backward_pass_ms": bwd_g, "fp16_forward_pass_ms": fwd_g16,
+        "updates_per_pass": U, "fp32_forward_updates_per_s": U / (fwd_g / 1e3),
+        "fp32_forward_GBps_21B": U * 21 / (fwd_g / 1e3) / 1e9,
+        "fp32_forward_frac_of_hbm": U * 21 / (fwd_g / 1e3) / 1e9 / load_peaks()[0],
+        "fp32_backward_GBps_17B": U * 17 / (bwd_g / 1e3) / 1e9}
+    del cost, m, am, sc, gin, ch, mh, jg, eg
     f0 = torch.randn((1, 32, 384, 512), device=dev)
     f1 = torch.randn((1, 32, 384, 512), device=dev)
     flow = timed(lambda: ops.flow_forward(f0, f1, 64))

@@ -358,7 +358,9 @@ def lbp_forward_f16(variant: int, cost_h: torch.Tensor, jump: torch.Tensor, edge
         if tuple(jump.shape) != (_pixel_planes(variant), H, W, L, Lp):
             raise BplError(f"pixel jump must be ({_pixel_planes(variant)},H,W,L,Lp) half, got {tuple(jump.shape)}")
     else:
-        raise BplError("FP16 storage serves the stereo and pixel variants")
+        _check_input("jump", jump, dim=4)
+        if tuple(jump.shape[1:]) != (4, L, L):
+            raise BplError(f"semantic jump must be (1,4,L,L) float, got {tuple(jump.shape)}")
     # argmin_dtype=None: no argmin is written (inference)
     kind = ARGMIN_NONE if argmin_dtype is None else _ARGMIN_KIND[argmin_dtype]
     if argmin is None and kind != ARGMIN_NONE:
@@ -399,13 +401,15 @@ def lbp_backward_f16(variant: int, jump, edge: torch.Tensor, in_grad_h: torch.Te
         grad_jump = torch.empty((_pixel_planes(variant), H, W, L, L), dtype=torch.float32, device=dev)
         grad_edge = None
     else:
-        raise BplError("FP16 storage serves the stereo and pixel variants")
+        _check_input("jump", jump, dim=4)
+        grad_jump = torch.empty((B, 4, L, L), dtype=torch.float32, device=dev)
+        grad_edge = torch.empty(tuple(edge.shape), dtype=torch.float32, device=dev)
     grad_cost = torch.empty((B, H, W, Lp), dtype=torch.float32, device=dev)
     need = lbp_backward_workspace_bytes(B, H, W, Lp)
     if workspace is None or workspace.numel() * workspace.element_size() < need:
         workspace = torch.empty(need, dtype=torch.uint8, device=dev)
     st = _timed("lbp_backward_f16", lambda: lib().bpl_lbp_backward_f16(
-        variant, _ptr(jump) if variant == LBP_STEREO else None, _ptr(edge), _ptr(in_grad_h), _ptr(messages_h),
+        variant, _ptr(jump) if not _pixel(variant) else None, _ptr(edge), _ptr(in_grad_h), _ptr(messages_h),
         _ptr(argmin), kind, _ptr(scale), _ptr(grad_cost), _ptr(grad_jump), _ptr(grad_edge), _ptr(workspace),
         workspace.numel() * workspace.element_size(), B, H, W, L, Lv, jb, edge.shape[0], _stream(messages_h)))
     check(st, "bpl_lbp_backward_f16")

@@ -81,9 +81,6 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
     BPL_REQUIRE(Lv >= 2 && Lv <= 16, "lbp_backward: Lv=%d outside [2, 16]", Lv);
     BPL_REQUIRE(jump_batch == 1 || jump_batch == B, "lbp_backward: jump batch %d must be 1 or B", jump_batch);
   }
-  if (variant == BPL_LBP_SEM_PIXEL) BPL_REQUIRE(L <= 96, "lbp_backward: pixel-pairwise variant supports L <= 96");
-  if (storage == 1)
-    BPL_REQUIRE(variant != BPL_LBP_SEM_GLOBAL, "lbp_backward_f16: FP16 storage serves the stereo and pixel variants");
 
   cudaStream_t s = as_stream(stream);
   const int64_t HW = static_cast<int64_t>(H) * W;
@@ -134,7 +131,9 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   a.am_bulk = (a.vec4 && (Ls * am_size) % 16 == 0) ? 1 : 0;
   a.ns = 0;  // rows are prefetched into registers: no shared-memory ring
   if (storage == 1)
-    return (variant == BPL_LBP_STEREO) ? lbp_backward_stereo_f16(a, s) : lbp_backward_sem_pixel_f16(a, s);
+    return (variant == BPL_LBP_STEREO)       ? lbp_backward_stereo_f16(a, s)
+           : (variant == BPL_LBP_SEM_GLOBAL) ? lbp_backward_sem_global_f16(a, s)
+                                             : lbp_backward_sem_pixel_f16(a, s);
   int st;
   switch (variant) {
     case BPL_LBP_STEREO: st = lbp_backward_stereo(a, s); break;

@@ -202,7 +202,12 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
   const bool stereo = (VARIANT == BPL_LBP_STEREO);
   // label validity: with K = ceil(L/32) (the K <= 8 instantiations are
   // dispatched exactly) only the last slot can hold labels >= L
-  auto lvalid = [&](int kk) -> bool { return (K <= 8 && kk < K - 1) || (lane + 32 * kk < L); };
+  // only the last slot can hold labels >= L when K = ceil(L/32) (the
+  // stereo and global dispatch is exact up to K = 8; the pixel variant's
+  // K = 8 and 32 serve several label counts and test every slot)
+  auto lvalid = [&](int kk) -> bool {
+    return (VARIANT != BPL_LBP_SEM_PIXEL && K <= 8 && kk < K - 1) || (lane + 32 * kk < L);
+  };
   const int nj = (a.jb == 1) ? 0 : n;
   const int ne = (a.eb == 1) ? 0 : n;
   const uint32_t am_size = (a.argmin_kind == BPL_ARGMIN_U8) ? 1u : (a.argmin_kind == BPL_ARGMIN_U16 ? 2u : 4u);
@@ -559,7 +564,9 @@ int dispatch_bwd(const BwdArgs& a, cudaStream_t s) {
   if constexpr (V == BPL_LBP_SEM_PIXEL) {
     if (k == 1) return launch_bwd_k<1, V, LV, T>(a, s);
     if (k == 2) return launch_bwd_k<2, V, LV, T>(a, s);
-    return launch_bwd_k<3, V, LV, T>(a, s);
+    if (k == 3) return launch_bwd_k<3, V, LV, T>(a, s);
+    if (k <= 8) return launch_bwd_k<8, V, LV, T>(a, s);
+    return launch_bwd_k<32, V, LV, T>(a, s);
   }
   switch (k) {
     case 1: return launch_bwd_k<1, V, LV, T>(a, s);
@@ -583,6 +590,7 @@ int lbp_backward_stereo_lv8(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_stereo(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_stereo_f16(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_sem_pixel_f16(const BwdArgs& a, cudaStream_t s);
+int lbp_backward_sem_global_f16(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_sem_global(const BwdArgs& a, cudaStream_t s);
 int lbp_backward_sem_pixel(const BwdArgs& a, cudaStream_t s);
 

@@ -36,10 +36,6 @@ int lbp_forward_impl(int storage, int variant, const void* cost, const void* jum
     BPL_REQUIRE(Lv >= 2 && Lv <= 16, "lbp_forward: Lv=%d outside [2, 16]", Lv);
     BPL_REQUIRE(jump_batch == 1 || jump_batch == B, "lbp_forward: jump batch %d must be 1 or B", jump_batch);
   }
-  if (variant == BPL_LBP_SEM_PIXEL)
-    BPL_REQUIRE(L <= 96, "lbp_forward: pixel-pairwise variant supports L <= 96");
-  if (storage == 1)
-    BPL_REQUIRE(variant != BPL_LBP_SEM_GLOBAL, "lbp_forward_f16: FP16 storage serves the stereo and pixel variants");
 
   FwdArgs a{};
   a.cost = cost;
@@ -64,22 +60,27 @@ int lbp_forward_impl(int storage, int variant, const void* cost, const void* jum
     a.Lm = L;
     a.lmat = 0;
     a.vec4 = (L % 4 == 0) ? 1 : 0;
-    if (variant == BPL_LBP_SEM_PIXEL) {
+    if (variant == BPL_LBP_SEM_PIXEL && L <= kPixelRingMaxL) {
       a.lmat = align4(L * L);
       a.vec4 = a.vec4 && ((L * L) % 4 == 0);
     }
   } else {
     a.Ls = (L + 7) & ~7;
     a.Lm = a.Ls;
-    a.lmat = (variant == BPL_LBP_SEM_PIXEL) ? L * a.Lm : 0;
+    a.lmat = (variant == BPL_LBP_SEM_PIXEL && L <= kPixelRingMaxL) ? L * a.Lm : 0;
     a.vec4 = 1;
   }
-  // shared-memory ring (pixel variant only): 4 steps in flight, one step
-  // per mbarrier group; the other variants prefetch rows into registers
-  a.ns = (variant == BPL_LBP_SEM_PIXEL) ? (a.vec4 ? 4 : kRingCpAsync) : 0;
+  // shared-memory ring (pixel variant up to kPixelRingMaxL labels): 4 steps
+  // in flight, one step per mbarrier group; the other variants, and wider
+  // pixel rows, prefetch rows into registers (wider pixel rows read their
+  // matrices from global memory)
+  a.ns = (variant == BPL_LBP_SEM_PIXEL && L <= kPixelRingMaxL) ? (a.vec4 ? 4 : kRingCpAsync) : 0;
   a.sps = 1;
   cudaStream_t s = as_stream(stream);
-  if (storage == 1) return (variant == BPL_LBP_STEREO) ? lbp_forward_stereo_f16(a, s) : lbp_forward_sem_pixel_f16(a, s);
+  if (storage == 1) {
+    if (variant == BPL_LBP_STEREO) return lbp_forward_stereo_f16(a, s);
+    return (variant == BPL_LBP_SEM_GLOBAL) ? lbp_forward_sem_global_f16(a, s) : lbp_forward_sem_pixel_f16(a, s);
+  }
   switch (variant) {
     case BPL_LBP_STEREO: return lbp_forward_stereo(a, s);
     case BPL_LBP_SEM_GLOBAL: return lbp_forward_sem_global(a, s);

@@ -42,6 +42,10 @@ namespace bpl {
 // cp.async.wait_group)
 constexpr int kRingCpAsync = 4;
 
+// largest label count of the pixel-pairwise variant whose per-pixel L x L
+// matrices are staged through the shared-memory ring (K <= 3 slots)
+constexpr int kPixelRingMaxL = 96;
+
 // largest truncation half-width served by the unrolled zero-offset window
 constexpr int kFastDelta = 4;
 // +inf padding on each side of the per-warp h row
@@ -447,10 +451,14 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
     c.pt = tr ? a.Lm : 1;
   }
   c.t0 = 32 * KW * wic;
-  // label validity: with K = ceil(L/32) (the K <= 8 instantiations are
-  // dispatched exactly) only the last slot of a one-warp scanline can hold
-  // labels >= L; the test folds away for the other slots
-  auto lvalid = [&](int kk) -> bool { return (K <= 8 && NW == 1 && kk < KW - 1) || (c.t0 + lane + 32 * kk < L); };
+  // label validity: with K = ceil(L/32) (the stereo K <= 8 instantiations
+  // are dispatched exactly) only the last slot of a one-warp scanline can
+  // hold labels >= L; the test folds away for the other slots.  The semantic
+  // variants share instantiations between label counts (K = 8 serves 129..256)
+  // and test every slot.
+  auto lvalid = [&](int kk) -> bool {
+    return (VARIANT == BPL_LBP_STEREO && K <= 8 && NW == 1 && kk < KW - 1) || (c.t0 + lane + 32 * kk < L);
+  };
   // labels copied per row: the warp's labels below Ls (padding included, so
   // half rows stay 16-byte sized)
   c.cnt = max(0, min(lroww, Ls - c.t0));
@@ -458,12 +466,25 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
   const float* gjump =
       (VARIANT == BPL_LBP_SEM_GLOBAL) ? static_cast<const float*>(a.jump) + static_cast<int64_t>(c.dir) * L * L : nullptr;
   const bool stereo = (VARIANT == BPL_LBP_STEREO);
+  // Global pairwise with one label per lane (L <= 32): the lane's column of
+  // the direction's matrix, P[s][t] for its label t, held in registers for
+  // the whole scanline, so the full minimisation is L register FMAs against
+  // broadcast reads of h instead of L global (L1) loads per step.
+  constexpr bool kPcolRegs = (VARIANT == BPL_LBP_SEM_GLOBAL) && K == 1 && NW == 1;
+  float pcol[kPcolRegs ? 32 : 1];
+  if constexpr (kPcolRegs) {
+#pragma unroll
+    for (int s = 0; s < 32; ++s) pcol[s] = (s < L && lane < L) ? __ldg(gjump + s * L + lane) : 0.0f;
+  }
 
   // Pixel variant: a shared-memory ring of the steps' rows and L x L
   // matrices (groups of sps steps, one mbarrier each).  Other variants: the
   // next step's own rows are prefetched into registers (coalesced loads of
   // data no sweep of this phase writes), one step ahead.
-  constexpr bool kRing = (VARIANT == BPL_LBP_SEM_PIXEL);
+  // (pixel variant above 96 labels: a sender's L x L matrix no longer fits
+  // a ring stage, so its entries are read from global memory as used)
+  constexpr bool kRing = (VARIANT == BPL_LBP_SEM_PIXEL) && K <= 3;
+  constexpr bool kPixGlobal = (VARIANT == BPL_LBP_SEM_PIXEL) && !kRing;
   const int G = kRing ? a.sps : 1;
   T ncst[KW], nva[KW], nvb[KW];  // raw: converted when used, so the loads do not stall here
   auto prefetch = [&](int i) {
@@ -522,6 +543,17 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
     const int b = i >> 5;
     const float* tile = sm.taps + (b & 1) * tile_stride;
     const T* stg = reinterpret_cast<const T*>(sm.ring) + st * sf;
+    // the sender's pairwise entry f(t, s): staged (ring) or read from global
+    // memory (wide pixel rows; the first sender of a shifted direction reads
+    // the layer's zero matrix)
+    const T* pmat = nullptr;
+    if constexpr (kPixGlobal)
+      pmat = (c.pshift != 0 && i == 0) ? nullptr : c.pjump + static_cast<int64_t>(pin + c.pshift) * L * a.Lm;
+    auto pairf = [&](int s_, int t_) -> float {
+      if constexpr (kRing) return ldf<T>(stg[3 * lroww + s_ * c.ps + t_ * c.pt]);
+      else if constexpr (kPixGlobal) return pmat ? ldf<T>(pmat[s_ * c.ps + t_ * c.pt]) : 0.0f;
+      else return 0.0f;
+    };
 
     // wait for the ring group of step i (own labels) at its first step
     const int grp = st / G;
@@ -613,7 +645,28 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
     }
     auto earg = [ref](float x) { return kExact ? x : __fsub_rn(x, ref); };
 
-    if (delta >= L) {
+    if (kPcolRegs && delta >= L) {
+      // full minimisation with the register column (see kPcolRegs); same
+      // order and tie rule as below
+      float m = 1e15f;
+      int arg = 0;
+#pragma unroll
+      for (int s = 0; s < 32; ++s) {
+        if (s < L) {
+          const float nm = __fmaf_rn(pcol[s], w, cs.hs[s]);
+          m = fminf(m, nm);
+          if (m == nm) arg = s;
+        }
+      }
+      msg[0] = (lane < L) ? m : 1e15f;
+      am[0] = (lane < L) ? arg : 0;
+      bool eok0 = exp_try<kExact>(earg(msg[0]), e[0], s_ehi, s_elo);
+      if (lane >= L) {
+        e[0] = 0.0f;
+        eok0 = true;
+      }
+      if (!__all_sync(FULL, eok0) && !eok0) e[0] = static_cast<float>(exp(static_cast<double>(msg[0])));
+    } else if (delta >= L) {
       // full minimisation (lbp_min_sum_kernel.cu:88-111): last minimiser wins
 #pragma unroll
       for (int kk = 0; kk < KW; ++kk) {
@@ -629,7 +682,7 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
             } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
               f = __ldg(gjump + s * L + t);
             } else {
-              f = ldf<T>(stg[3 * lroww + s * c.ps + t * c.pt]);
+              f = pairf(s, t);
             }
             const float nm = __fmaf_rn(f, w, cs.hs[s]);
             m = fminf(m, nm);
@@ -672,7 +725,7 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
       } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
         L2 = __ldg(gjump + (L - 1));
       } else {
-        L2 = ldf<T>(stg[3 * lroww + (L - 1) * c.pt]);
+        L2 = pairf(0, L - 1);
       }
       // The global candidate needs only the minimum value of h, which any
       // reduction order gives exactly.
@@ -874,7 +927,7 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
               } else if (VARIANT == BPL_LBP_SEM_GLOBAL) {
                 f = __ldg(gjump + s * L + t);
               } else {
-                f = ldf<T>(stg[3 * lroww + s * c.ps + t * c.pt]);
+                f = pairf(s, t);
               }
               const float nm = __fmaf_rn(f, w, cs.hs[s]);
               if (nm <= m) {
@@ -1063,7 +1116,7 @@ template <int K, int V, int NW, typename T>
 int launch_phase(const FwdArgs& a0, cudaStream_t stream) {
   FwdArgs a = a0;
   const int lroww = 32 * (K / NW);
-  if (V == BPL_LBP_SEM_PIXEL && NW == 1 && a.nchains > kHiOccChainsPerSm * sm_count()) {
+  if (V == BPL_LBP_SEM_PIXEL && NW == 1 && a.ns > 0 && a.nchains > kHiOccChainsPerSm * sm_count()) {
     // one-warp blocks: the deepest ring (4..2 steps) whose shared memory lets
     // every scanline of the phase be resident at once; a second, partial
     // wave of full-length scanlines costs more than a shallower prefetch
@@ -1132,10 +1185,13 @@ int dispatch_k(const FwdArgs& a, cudaStream_t s) {
   if constexpr (V != BPL_LBP_STEREO) {
     // semantic variants: one warp per scanline
     if constexpr (V == BPL_LBP_SEM_PIXEL) {
-      // per-pixel L x L matrices: L <= 96 (checked at the entry point)
+      // per-pixel L x L matrices: staged through the ring up to L = 96,
+      // read from global memory above
       if (k == 1) return launch_k<1, V, 1, 1, T>(a, s);
       if (k == 2) return launch_k<2, V, 2, 1, T>(a, s);
-      return launch_k<3, V, 3, 1, T>(a, s);
+      if (k == 3) return launch_k<3, V, 3, 1, T>(a, s);
+      if (k <= 8) return launch_k<8, V, 8, 1, T>(a, s);
+      return launch_k<32, V, 32, 1, T>(a, s);
     }
     switch (k) {
       case 1: return launch_k<1, V, 1, 1, T>(a, s);
@@ -1173,5 +1229,6 @@ int lbp_forward_sem_global(const FwdArgs& a, cudaStream_t s);
 int lbp_forward_sem_pixel(const FwdArgs& a, cudaStream_t s);
 int lbp_forward_stereo_f16(const FwdArgs& a, cudaStream_t s);
 int lbp_forward_sem_pixel_f16(const FwdArgs& a, cudaStream_t s);
+int lbp_forward_sem_global_f16(const FwdArgs& a, cudaStream_t s);
 
 }  // namespace bpl

@@ -117,9 +117,13 @@ int bpl_lbp_forward(int variant, const float* cost, const float* jump, const flo
  * labels near the row's minimum.
  * Layout: the label axis has stride Lp = L rounded up to 8 (16-byte rows):
  *   cost (B,H,W,Lp) half, messages (B,4,H,W,Lp) half, argmin (B,4,H,W,Lp),
- *   pixel-pairwise jump (4,H,W,L,Lp) half; stereo jump taps, edge and scale
- *   stay float.  Labels L..Lp-1 are ignored on input and not written.
- * Variants: BPL_LBP_STEREO and BPL_LBP_SEM_PIXEL.
+ *   pixel-pairwise jump (4,H,W,L,Lp) half; stereo jump taps, the semantic
+ *   global jump (1,4,L,L), edge and scale stay float.  Labels L..Lp-1 are
+ *   ignored on input and not written.
+ * scale may be NULL: it is then not computed (the FP16 adjoint recomputes
+ * the normalisation from the rows), and the stereo kernel's step carries no
+ * exp at all.
+ * Variants: all (BPL_LBP_STEREO, BPL_LBP_SEM_GLOBAL, BPL_LBP_SEM_PIXEL[_LAYER]).
  */
 int bpl_lbp_forward_f16(int variant, const void* cost, const void* jump, const float* edge,
                         void* messages, void* argmin, int argmin_kind, float* scale, int B, int H,
@@ -306,8 +310,11 @@ int bpl_sad_volume_depth(int min_disp, int max_disp, float step);
  * messages and scale as bpl_lbp_forward_f16 wrote them (min-referenced rows);
  * argmin (B,4,H,W,Lp); grad_cost (B,H,W,Lp) float (labels >= L are zero);
  * grad_jump / grad_edge as bpl_lbp_backward (float, unpadded).  workspace:
- * bpl_lbp_backward_workspace_size(B, H, W, Lp) bytes.  Variants
- * BPL_LBP_STEREO and BPL_LBP_SEM_PIXEL.
+ * bpl_lbp_backward_workspace_size(B, H, W, Lp) bytes.  The normalisation's
+ * Jacobian uses the softmax of each message row as it is now (the
+ * reference's exp(m_raw)/S with m_raw rebuilt from the saved message and
+ * log S is the softmax of the saved message, whichever pass S came from),
+ * so scale is not read and may be NULL.  All variants.
  */
 int bpl_lbp_backward_f16(int variant, const float* jump, const float* edge, const void* in_grad,
                          const void* messages, const void* argmin, int argmin_kind, const float* scale,

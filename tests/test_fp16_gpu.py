@@ -19,7 +19,8 @@ def _labels(msgs, cost):
 
 
 @pytest.mark.parametrize("case", [("stereo_l96", 0, 1, 40, 64, 96, 3), ("stereo_l64_b2", 0, 2, 24, 40, 64, 2),
-                                  ("pixel_l19", 2, 1, 32, 48, 19, 2)], ids=lambda c: c[0])
+                                  ("pixel_l19", 2, 1, 32, 48, 19, 2), ("global_l19", 1, 2, 32, 48, 19, 2)],
+                         ids=lambda c: c[0])
 def test_fp16_forward_against_fp64_oracle(case):
     from bpl_gb300 import ops
     name, variant, B, H, W, L, iters = case
@@ -28,6 +29,10 @@ def test_fp16_forward_against_fp64_oracle(case):
     if variant == 0:
         cost, *_ = cases.stereo_cost_from_scene(g, B, H, W, 16, L)
         jump = cases.stereo_taps(1, H, W, 0.1, 0.5)
+        jt = torch.from_numpy(jump).to(dev)
+    elif variant == 1:
+        cost = cases.random_cost(g, B, H, W, L)
+        jump, _ = cases.semantic_global_jump(g, L)
         jt = torch.from_numpy(jump).to(dev)
     else:
         cost = cases.random_cost(g, B, H, W, L)
@@ -48,7 +53,7 @@ def test_fp16_forward_against_fp64_oracle(case):
     assert torch.allclose(torch.log(sc[written]), lse[written], rtol=0, atol=1e-3)
     # FP64 oracle on the same (half-rounded) inputs
     cost_r = ch[..., :L].float().cpu().numpy().astype(np.float64)
-    jump_r = jump if variant == 0 else jt[..., :L].float().cpu().numpy()
+    jump_r = jump if variant in (0, 1) else jt[..., :L].float().cpu().numpy()
     m64, _, _ = oracle.lbp_forward(variant, cost_r, jump_r, edge, np.zeros((B, 4, H, W, L)), delta, fp64=True,
                                    iters=iters)
     lab16 = _labels(m16.astype(np.float64), cost_r)

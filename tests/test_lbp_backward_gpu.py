@@ -3,8 +3,14 @@ against the oracle's double-precision restatement of the reference backward
 (ops/lbp_stereo/src/lbp_min_sum_kernel.cu:215-417, :513-621).
 
 The reference itself accumulates with float atomics in arbitrary order, so the
-bar is a tolerance: max |gpu - oracle| <= 2e-4 * max |oracle| per tensor
-(float32 accumulation over chains of up to W steps), grad_messages exact.
+bar is a tolerance, per element: |gpu - oracle| <= ATOL * max|oracle| +
+RTOL * |oracle| for every element of each tensor (float32 accumulation over
+chains of up to W steps: an entry whose terms cancel keeps an absolute error
+on the scale of the tensor), and max |gpu - oracle| <= 2e-4 * max |oracle|;
+grad_messages exact.  (At the full size this library's adjoint is measured
+against the reference op itself in test_reference_ops_gpu.py: its largest
+error against the double-precision adjoint is about 2e-6 of the tensor's
+scale, the reference op's about 3e-5.)
 """
 import numpy as np
 import pytest
@@ -16,10 +22,18 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 TOL = 2e-4
+ATOL = 1e-5
+RTOL = 1e-4
 
 
 def rel_err(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-12))
+
+
+def assert_elementwise(a, b, what):
+    lim = ATOL * max(np.abs(b).max(), 1e-30) + RTOL * np.abs(b)
+    bad = np.abs(a - b) > lim
+    assert not bad.any(), f"{what}: {int(bad.sum())} of {b.size} elements outside atol+rtol*|ref|"
 
 
 def run_case(variant, cost, jump, edge, msgs, delta, gin, argmin_dtype=torch.float32):
@@ -46,8 +60,11 @@ def check(variant, fwd, bwd, jump, edge, gin, name):
         re_ = re_.sum(0, keepdims=True)
     assert rel_err(bwd[0], rc) <= TOL, f"{name} grad_cost {rel_err(bwd[0], rc):.2e}"
     assert rel_err(bwd[1], rj) <= TOL, f"{name} grad_jump {rel_err(bwd[1], rj):.2e}"
+    assert_elementwise(bwd[0], rc, f"{name} grad_cost")
+    assert_elementwise(bwd[1], rj, f"{name} grad_jump")
     if variant != 2:
         assert rel_err(bwd[2], re_) <= TOL, f"{name} grad_edge {rel_err(bwd[2], re_):.2e}"
+        assert_elementwise(bwd[2], re_, f"{name} grad_edge")
     np.testing.assert_array_equal(bwd[3], gin)
 
 
@@ -94,7 +111,9 @@ def test_backward_compact_argmin(dtype):
 
 SEM = [("global_l19", 1, 31, 1, 10, 12, 19, 19), ("global_l19_b2", 1, 32, 2, 8, 11, 19, 3),
        ("global_l40", 1, 33, 1, 6, 9, 40, 40), ("pixel_l7", 2, 41, 1, 8, 10, 7, 7),
-       ("pixel_l19_b2", 2, 42, 2, 9, 13, 19, 19), ("pixel_l8", 2, 43, 1, 6, 7, 8, 8)]
+       ("pixel_l19_b2", 2, 42, 2, 9, 13, 19, 19), ("pixel_l8", 2, 43, 1, 6, 7, 8, 8),
+       ("global_l150_k8", 1, 34, 1, 5, 7, 150, 150), ("pixel_l100_global_reads", 2, 44, 1, 5, 6, 100, 100),
+       ("pixel_l130_trunc", 2, 45, 1, 4, 5, 130, 4)]
 
 
 @pytest.mark.parametrize("case", SEM, ids=[c[0] for c in SEM])

@@ -116,7 +116,10 @@ def test_compact_argmin_matches_float(dtype):
 
 
 SEM_CASES = [("global_l19", 1, 31, 2, 10, 12, 19, 19), ("global_l19_trunc", 1, 32, 1, 8, 11, 19, 3),
-             ("global_l40", 1, 33, 1, 6, 9, 40, 40), ("pixel_l7", 2, 41, 1, 8, 10, 7, 7),
+             ("global_l40", 1, 33, 1, 6, 9, 40, 40), ("global_l32_regs", 1, 34, 1, 7, 9, 32, 32),
+             ("global_l1", 1, 35, 1, 5, 6, 1, 1), ("global_l31_many_chains", 1, 36, 2, 96, 128, 31, 31),
+             ("global_l150_k8", 1, 37, 1, 5, 7, 150, 150), ("pixel_l100_global_reads", 2, 44, 1, 5, 6, 100, 100),
+             ("pixel_l130_trunc", 2, 45, 1, 4, 5, 130, 4), ("pixel_l300_k32", 2, 46, 1, 3, 4, 300, 300), ("pixel_l7", 2, 41, 1, 8, 10, 7, 7),
              ("pixel_l19", 2, 42, 2, 9, 13, 19, 19), ("pixel_l8_trunc", 2, 43, 1, 6, 7, 8, 2)]
 
 

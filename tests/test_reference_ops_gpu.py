@@ -514,7 +514,10 @@ def test_reference_sad_and_flow_wrappers_run_unchanged_on_this_library(ref):
                           flow_mod)
         a, b = f0.clone().requires_grad_(True), f1.clone().requires_grad_(True)
         cu, cv, us, vs = w.FlowMpSadFunction.apply(a, b, 16)
-        (cu.sum() + 2.0 * cv.sum()).backward()
+        # contiguous upstream gradients (the reference op requires them)
+        gu = torch.randn(cu.shape, device=dev(), generator=gen(82))
+        gv = torch.randn(cv.shape, device=dev(), generator=gen(83))
+        torch.autograd.backward([cu, cv], [gu, gv])
         torch.cuda.synchronize()
         res.append((cu.detach(), cv.detach(), us, vs, a.grad, b.grad))
     for nm, x, y in zip(("cv_u", "cv_v", "u_star", "v_star", "df0"), res[1][:5], res[0][:5]):
