@@ -1028,7 +1028,7 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
       }
     }
 
-    if (VARIANT == BPL_LBP_SEM_PIXEL) {
+    if constexpr (kRing) {
       __syncwarp();
       if (st == grp * G + G - 1 && issue_group<VARIANT, T>(a, c, sm, lroww, i + 1 - G + a.ns, grp, nsteps, lane))
         armed |= 1u << grp;

@@ -126,12 +126,15 @@ def test_recompute_argmin_variant_matches_stored(adjoint, storage, size):
         # both variants hold the cost volume (for the belief epilogue) and the
         # pairwise taps; beyond those, the storing variant holds the indices
         # (and the FP32 scales), the recomputing one the two initial slots
+        # (and, FP16, the half copy of the cost that its re-run reads)
         Ls = ops_padded(L) if storage == "fp16" else L
         argmin_bytes = iters * B * 4 * H * W * Ls
         vert_bytes = 2 * B * H * W * Ls * (2 if storage == "fp16" else 4)
+        if storage == "fp16":
+            vert_bytes += B * H * W * Ls * 2
         print(f"{storage} held by the forward: stored indices {held[0] / 2**20:.1f} MiB, "
               f"recompute {held[1] / 2**20:.1f} MiB (indices {argmin_bytes / 2**20:.1f} MiB, "
-              f"initial vertical slots {vert_bytes / 2**20:.1f} MiB)")
+              f"kept for the re-run {vert_bytes / 2**20:.1f} MiB)")
         assert vert_bytes < argmin_bytes
         assert held[0] - held[1] >= argmin_bytes - vert_bytes
     (b0, gp0, ge0, l10, l20), (b1, gp1, ge1, l11, l21) = grads
