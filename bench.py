@@ -863,8 +863,11 @@ def run_ncu_case(args):
     size limit), the exact adjoint's message-gradient assembly, the belief
     epilogue, SAD at 384x512 C=64 D=192, the flow SAD at 384x512 C=32,
     window +-32, the coarse-to-fine glue into 256x512x192, the slot
-    broadcast of a 256x512x192 volume and the semantic pixel-pairwise
-    forward at 512x1024, L=19 (the layer's two pairwise planes)."""
+    broadcast of a 256x512x192 volume, the semantic pixel-pairwise
+    forward at 512x1024, L=19 (the layer's two pairwise planes), the FP16
+    stereo forward at 256x512x192, the semantic global forward at
+    512x1024, L=19, and the epilogue kernels (cost from the 384x512x192
+    SAD volume, disparity from the FP16 messages)."""
     import torch
     from bpl_gb300 import ops
     import cases
@@ -886,6 +889,12 @@ def run_ncu_case(args):
     pjp = torch.rand((2, 2 * h, 2 * w, 19, 19), device=dev)
     pedge = torch.ones((1, 4, 2 * h, 2 * w), device=dev)
     pm = torch.zeros((1, 4, 2 * h, 2 * w, 19), device=dev)
+    # FP16 storage (the lean stereo kernel) and the semantic global form
+    ch = ops.to_half_padded(cost, L)
+    mh = torch.zeros((1, 4, h, w, ops.padded_labels(L)), dtype=torch.float16, device=dev)
+    gP = torch.rand((1, 4, 19, 19), device=dev)
+    gm = torch.zeros((1, 4, 2 * h, 2 * w, 19), device=dev)
+    gh = ops.to_half_padded(gin, L)
     for it in range(2):
         if it == 1:
             torch.cuda.synchronize()
@@ -902,6 +911,11 @@ def run_ncu_case(args):
         ops.upsample_add_beliefs(bc, pvl, 0.5)
         ops.broadcast_slots(cost)
         ops.lbp_forward(ops.LBP_SEM_PIXEL_LAYER, pcost, pjp, pedge, pm, 19, argmin_dtype=torch.uint8)
+        _, amh, _ = ops.lbp_forward_f16(ops.LBP_STEREO, ch, jump, edge, mh, DELTA, L, argmin_dtype=torch.uint8)
+        ops.lbp_backward_passes(ops.LBP_STEREO, jump, edge, gh, mh, amh.unsqueeze(0), None, L=L)
+        ops.lbp_forward(ops.LBP_SEM_GLOBAL, pcost, gP, pedge, gm, 19, argmin_dtype=torch.uint8)
+        ops.cost_from_sad(vol, 1.0, half=True)
+        ops.messages_argmin(mh, ch, L)
         torch.cuda.synchronize()
     torch.cuda.profiler.stop()
     print(json.dumps({"ncu_case": f"{h}x{w}x{L}", "updates_per_pass": L * edges(h, w)}))

@@ -569,6 +569,8 @@ def cost_from_sad(sad: torch.Tensor, temperature: float = 1.0, half: bool = Fals
     with the label axis padded to a multiple of 8 (padding zeroed)."""
     _check_input("sad", sad, dim=4)
     B, H, W, D = sad.shape
+    if not temperature > 0:
+        raise BplError("temperature must be positive")
     Ls = padded_labels(D) if half else D
     dtype = torch.float16 if half else torch.float32
     if out is None:
@@ -590,7 +592,12 @@ def messages_argmin(messages: torch.Tensor, cost: torch.Tensor, L: int | None = 
     _check_input("cost", cost, dtype=None, dim=4)
     B, _, H, W, Ls = messages.shape
     Lc = cost.shape[-1]
+    if messages.shape[1] != 4 or tuple(cost.shape[:3]) != (B, H, W):
+        raise BplError(f"messages (B,4,H,W,Ls) and cost (B,H,W,Lc) disagree: {tuple(messages.shape)} / "
+                       f"{tuple(cost.shape)}")
     L = min(Ls, Lc) if L is None else int(L)
+    if L < 1 or L > min(Ls, Lc):
+        raise BplError(f"L={L} outside the rows (messages {Ls}, cost {Lc})")
     for nm, t in (("messages", messages), ("cost", cost)):
         if t.dtype not in (torch.float32, torch.float16):
             raise BplError(f"{nm} must be float32 or float16")
