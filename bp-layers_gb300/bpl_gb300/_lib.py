@@ -44,6 +44,8 @@ SIGNATURES = {
     "bpl_cost_from_sad": [c_void_p, c_void_p, c_int] + [c_int] * 5 + [c_float, c_void_p],
     "bpl_messages_argmin": [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int] + [c_int] * 6 + [c_void_p],
     "bpl_beliefs_infer": [c_void_p, c_int, c_int, c_void_p] + [c_int] * 4 + [c_void_p],
+    "bpl_pack_taps": [c_void_p] * 3 + [c_int] * 4 + [c_void_p],
+    "bpl_unpack_tap_grad": [c_void_p] * 3 + [c_int] * 4 + [c_void_p],
     "bpl_lbp_backward_noalloc": [c_int] + [c_void_p] * 5 + [c_int] + [c_void_p] * 4 + [c_int] * 7 + [c_void_p],
 }
 _RESTYPE = {"bpl_status_string": ctypes.c_char_p, "bpl_last_error": ctypes.c_char_p,

@@ -69,38 +69,15 @@ def pack_affinities(affinities, offset):
     """(N,4,K,H,W) affinities [L2-, L2+, L1-, L1+, L3] (or [L1, L1, L2]) plus
     offset (N,4,H,W) -> (N,4,K+3,H,W) jump taps [offset, L3, L2-, L1-, 0, L1+,
     L2+, L3] with the reverse directions' +/- swapped
-    (message_passing_op_cuda.py:35-60)."""
-    N, D, K, H, W = affinities.shape
-    out = torch.zeros((N, D, K + 3, H, W), dtype=affinities.dtype, device=affinities.device)
-    out[:, :, 0] = offset
-    out[:, :, 1] = affinities[:, :, -1]
-    out[:, :, -1] = affinities[:, :, -1]
-    out[:, :, (K + 3) // 2] = 0.0
-    ic = 0
-    for i in range(2, (K + 3) // 2):
-        out[:, 0::2, i] = affinities[:, 0::2, ic]
-        out[:, 0::2, -i] = affinities[:, 0::2, ic + 1]
-        out[:, 1::2, i] = affinities[:, 1::2, ic + 1]
-        out[:, 1::2, -i] = affinities[:, 1::2, ic]
-        ic += 2
-    return out.contiguous()
+    (message_passing_op_cuda.py:35-60), in one kernel pass (ops.pack_taps)."""
+    return ops.pack_taps(affinities, offset)
 
 
 def unpack_affinity_grad(grad_taps):
-    """Inverse of pack_affinities for the gradient (message_passing_op_cuda.py:75-93).
-    Returns (grad_affinities (N,4,K,H,W), grad_offset (N,4,H,W))."""
-    N, D, Kp, H, W = grad_taps.shape
-    g = torch.zeros((N, D, Kp - 3, H, W), dtype=grad_taps.dtype, device=grad_taps.device)
-    g[:, :, -1] += grad_taps[:, :, 1]
-    g[:, :, -1] += grad_taps[:, :, -1]
-    ic = 0
-    for i in range(2, Kp // 2):
-        g[:, 0::2, ic] = grad_taps[:, 0::2, i]
-        g[:, 0::2, ic + 1] = grad_taps[:, 0::2, -i]
-        g[:, 1::2, ic + 1] = grad_taps[:, 1::2, i]
-        g[:, 1::2, ic] = grad_taps[:, 1::2, -i]
-        ic += 2
-    return g, grad_taps[:, :, 0]
+    """Inverse of pack_affinities for the gradient (message_passing_op_cuda.py:75-93),
+    in one kernel pass (ops.unpack_tap_grad).  Returns (grad_affinities
+    (N,4,K,H,W), grad_offset (N,4,H,W))."""
+    return ops.unpack_tap_grad(grad_taps)
 
 
 class LBPMinSumFunction(torch.autograd.Function):

@@ -624,3 +624,33 @@ def beliefs_infer(beliefs: torch.Tensor, mode: str = "wta", support: int = 3) ->
         _ptr(beliefs), 0 if mode == "wta" else 1, int(support), _ptr(out), B, H, W, L, _stream(beliefs)))
     check(st, "bpl_beliefs_infer")
     return out
+
+
+def pack_taps(affinities: torch.Tensor, offset: torch.Tensor) -> torch.Tensor:
+    """(N,4,K,H,W) affinities + (N,4,H,W) offset -> (N,4,K+3,H,W) stereo
+    jump taps, one kernel pass (message_passing_op_cuda.py:35-60)."""
+    affinities = affinities.detach().float().contiguous()
+    N, D, K, H, W = affinities.shape
+    if D != 4:
+        raise BplError(f"affinities must be (N,4,K,H,W), got {tuple(affinities.shape)}")
+    offset = offset.detach().float().to(affinities.device).expand(N, 4, H, W).contiguous()
+    _check_input("affinities", affinities, dim=5)
+    taps = torch.empty((N, 4, K + 3, H, W), dtype=torch.float32, device=affinities.device)
+    st = _timed("pack_taps", lambda: lib().bpl_pack_taps(
+        _ptr(affinities), _ptr(offset), _ptr(taps), N, K, H, W, _stream(affinities)))
+    check(st, "bpl_pack_taps")
+    return taps
+
+
+def unpack_tap_grad(grad_taps: torch.Tensor):
+    """Gradient fold of pack_taps: (grad_affinities (N,4,K,H,W), grad_offset
+    (N,4,H,W)), one kernel pass (message_passing_op_cuda.py:75-93)."""
+    grad_taps = grad_taps.contiguous()
+    _check_input("grad_taps", grad_taps, dim=5)
+    N, D, Kp, H, W = grad_taps.shape
+    gaff = torch.empty((N, 4, Kp - 3, H, W), dtype=torch.float32, device=grad_taps.device)
+    goff = torch.empty((N, 4, H, W), dtype=torch.float32, device=grad_taps.device)
+    st = _timed("unpack_tap_grad", lambda: lib().bpl_unpack_tap_grad(
+        _ptr(grad_taps), _ptr(gaff), _ptr(goff), N, Kp - 3, H, W, _stream(grad_taps)))
+    check(st, "bpl_unpack_tap_grad")
+    return gaff, goff

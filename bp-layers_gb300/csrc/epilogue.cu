@@ -12,6 +12,7 @@
 //       ties two labels
 //   wta / sub-exp on beliefs         inference_op.py:22-27, :53-97
 #include <cuda_fp16.h>
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include "bpl_device.cuh"
@@ -129,6 +130,65 @@ __global__ void __launch_bounds__(32 * kEpiWarps) beliefs_infer_kernel(const flo
 
 inline unsigned blocks_for(int64_t npix) { return static_cast<unsigned>((npix + kEpiWarps - 1) / kEpiWarps); }
 
+// Stereo jump taps from affinities (message_passing_op_cuda.py:35-60): for
+// K affinities [.., L3] per direction and Kp = K + 3 taps,
+//   tap 0 = offset, taps 1 and Kp-1 = the last affinity (L3), tap Kp/2 = 0,
+//   tap i in [2, Kp/2): affinity 2(i-2) on directions 0, 2 (LR, UD) and
+//   2(i-2)+1 on directions 1, 3 (RL, DU); tap Kp-i: the other one of the pair.
+// Returns the affinity index of tap i of direction d, -1 for the offset,
+// -2 for the zero centre tap.
+__device__ __forceinline__ int tap_source(int i, int d, int K) {
+  const int Kp = K + 3, c = Kp / 2;
+  if (i == 0) return -1;
+  if (i == c) return -2;
+  if (i == 1 || i == Kp - 1) return K - 1;
+  const bool mirror = i > c;
+  const int m = mirror ? Kp - i - 2 : i - 2;
+  const bool first = mirror == ((d & 1) != 0);  // LR/UD: i takes the pair's first, Kp-i its second
+  return 2 * m + (first ? 0 : 1);
+}
+
+// one thread per (n, d, pixel): taps[n,d,:,p] from aff[n,d,:,p] and offset[n,d,p]
+__global__ void pack_taps_kernel(const float* __restrict__ aff, const float* __restrict__ off, float* __restrict__ taps,
+                                 int N, int K, int64_t HW) {
+  const int64_t total = static_cast<int64_t>(N) * 4 * HW;
+  const int Kp = K + 3;
+  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < total;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t nd = e / HW, p = e % HW;
+    const int d = static_cast<int>(nd & 3);
+    const float* a = aff + nd * K * HW + p;
+    float* t = taps + nd * Kp * HW + p;
+    for (int i = 0; i < Kp; ++i) {
+      const int src = tap_source(i, d, K);
+      t[i * HW] = (src == -1) ? __ldg(off + e) : (src == -2 ? 0.0f : __ldg(a + src * HW));
+    }
+  }
+}
+
+// the fold of the tap gradient (message_passing_op_cuda.py:75-93): each
+// affinity sums the gradients of the taps it fills (L3: taps 1 and Kp-1,
+// added in that order), the offset takes tap 0, the centre tap is dropped
+__global__ void unpack_tap_grad_kernel(const float* __restrict__ gtaps, float* __restrict__ gaff,
+                                       float* __restrict__ goff, int N, int K, int64_t HW) {
+  const int64_t total = static_cast<int64_t>(N) * 4 * HW;
+  const int Kp = K + 3;
+  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < total;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t nd = e / HW, p = e % HW;
+    const int d = static_cast<int>(nd & 3);
+    const float* g = gtaps + nd * Kp * HW + p;
+    float* a = gaff + nd * K * HW + p;
+    for (int k = 0; k < K - 1; ++k) a[k * HW] = 0.0f;
+    a[(K - 1) * HW] = (0.0f + __ldg(g + HW)) + __ldg(g + (Kp - 1) * HW);
+    for (int i = 2; i < Kp - 1; ++i) {
+      const int src = tap_source(i, d, K);
+      if (src >= 0 && src != K - 1) a[src * HW] = __ldg(g + i * HW);
+    }
+    goff[e] = __ldg(g);
+  }
+}
+
 }  // namespace
 }  // namespace bpl
 
@@ -196,5 +256,31 @@ extern "C" int bpl_beliefs_infer(const float* beliefs, int mode, int support, vo
   else
     beliefs_infer_kernel<true><<<blocks_for(npix), 32 * kEpiWarps, 0, as_stream(stream)>>>(beliefs, out, npix, L, support);
   BPL_CUDA_TRY(cudaGetLastError(), "beliefs_infer launch");
+  return BPL_OK;
+}
+
+extern "C" int bpl_pack_taps(const float* affinities, const float* offset, float* taps, int N, int K, int H, int W,
+                             void* stream) {
+  BPL_TRACE("bpl_pack_taps");
+  BPL_REQUIRE(affinities && offset && taps, "pack_taps: null pointer");
+  BPL_REQUIRE(N >= 1 && H >= 1 && W >= 1, "pack_taps: bad shape");
+  BPL_REQUIRE(K >= 3 && K % 2 == 1 && K + 3 <= 16, "pack_taps: K=%d affinities (odd, 3..13) expected", K);
+  const int64_t HW = static_cast<int64_t>(H) * W, total = static_cast<int64_t>(N) * 4 * HW;
+  const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 152 * 16));
+  pack_taps_kernel<<<blocks, 256, 0, as_stream(stream)>>>(affinities, offset, taps, N, K, HW);
+  BPL_CUDA_TRY(cudaGetLastError(), "pack_taps launch");
+  return BPL_OK;
+}
+
+extern "C" int bpl_unpack_tap_grad(const float* grad_taps, float* grad_affinities, float* grad_offset, int N, int K,
+                                   int H, int W, void* stream) {
+  BPL_TRACE("bpl_unpack_tap_grad");
+  BPL_REQUIRE(grad_taps && grad_affinities && grad_offset, "unpack_tap_grad: null pointer");
+  BPL_REQUIRE(N >= 1 && H >= 1 && W >= 1, "unpack_tap_grad: bad shape");
+  BPL_REQUIRE(K >= 3 && K % 2 == 1 && K + 3 <= 16, "unpack_tap_grad: K=%d affinities (odd, 3..13) expected", K);
+  const int64_t HW = static_cast<int64_t>(H) * W, total = static_cast<int64_t>(N) * 4 * HW;
+  const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 152 * 16));
+  unpack_tap_grad_kernel<<<blocks, 256, 0, as_stream(stream)>>>(grad_taps, grad_affinities, grad_offset, N, K, HW);
+  BPL_CUDA_TRY(cudaGetLastError(), "unpack_tap_grad launch");
   return BPL_OK;
 }

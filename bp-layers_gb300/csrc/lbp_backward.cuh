@@ -200,9 +200,7 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
   }
   const int fd = db ^ 1;
   const bool stereo = (VARIANT == BPL_LBP_STEREO);
-  // label validity: with K = ceil(L/32) (the K <= 8 instantiations are
-  // dispatched exactly) only the last slot can hold labels >= L
-  // only the last slot can hold labels >= L when K = ceil(L/32) (the
+  // label validity: only the last slot can hold labels >= L when K = ceil(L/32) (the
   // stereo and global dispatch is exact up to K = 8; the pixel variant's
   // K = 8 and 32 serve several label counts and test every slot)
   auto lvalid = [&](int kk) -> bool {

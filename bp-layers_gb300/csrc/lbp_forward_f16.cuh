@@ -25,14 +25,32 @@
 // ops/lbp_stereo/src/lbp_min_sum_kernel.cu:55-164.
 #pragma once
 
+#include <type_traits>
+#include <utility>
+
 #include "lbp_forward.cuh"
 
 namespace bpl {
 
+// compile-time loop: f(integral_constant<int, 0>), ..., f(integral_constant<int, N-1>)
+template <typename F, int... I>
+__device__ __forceinline__ void static_for_impl(F& f, std::integer_sequence<int, I...>) {
+  (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
+
 template <int OCC>
 constexpr int f16_block_warps() { return (OCC > 1) ? 1 : 4; }
 
-template <int K, int OCC, bool SCALE>
+// PF: prefetch depth (steps whose rows are in flight).  The lean step is
+// short, so one step ahead does not cover a DRAM load (ncu: long-scoreboard
+// stalls led the one-ahead version); the 4-warp, latency-bound launch keeps
+// three steps in flight, the high-occupancy launch one (its other warps hide
+// the latency, and it has no registers to spare).
+template <int K, int OCC, bool SCALE, int PF>
 __global__ void __launch_bounds__(32 * f16_block_warps<OCC>(), OCC) lbp_forward_f16_kernel(FwdArgs a) {
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
@@ -90,18 +108,22 @@ __global__ void __launch_bounds__(32 * f16_block_warps<OCC>(), OCC) lbp_forward_
   auto lvalid = [&](int kk) -> bool { return kk < K - 1 || lane + 32 * kk < L; };
 
   // the next step's cost and cross-direction messages, one step ahead
-  __half ncst[K], nva[K], nvb[K];
-  auto prefetch = [&](int i) {
+  __half pcst[PF][K], pva[PF][K], pvb[PF][K];
+  auto prefetch = [&](auto SL, int i) {
+    constexpr int sl = decltype(SL)::value;
     const int64_t po = static_cast<int64_t>(c.pin0 + i * c.dpin) * Ls;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const int64_t o = po + (lvalid(kk) ? lane + 32 * kk : 0);
-      ncst[kk] = __ldg(cost + o);
-      nva[kk] = __ldg(slot_a + o);
-      nvb[kk] = __ldg(slot_b + o);
+      pcst[sl][kk] = __ldg(cost + o);
+      pva[sl][kk] = __ldg(slot_a + o);
+      pvb[sl][kk] = __ldg(slot_b + o);
     }
   };
-  prefetch(0);
+  static_for<PF>([&](auto SL) {
+    constexpr int s = decltype(SL)::value;
+    if (s < nsteps) prefetch(SL, s);
+  });
 
   float chain[K];
   {
@@ -120,8 +142,9 @@ __global__ void __launch_bounds__(32 * f16_block_warps<OCC>(), OCC) lbp_forward_
   const bool store_am = a.argmin_kind != BPL_ARGMIN_NONE;
   const float kInf = __int_as_float(0x7f800000);
   const int c0 = a.Lv / 2;
-  int pin = c.pin0;
-  for (int i = 0; i < nsteps; ++i, pin += c.dpin) {
+  auto step = [&](auto SL, const int i) {
+    constexpr int sl = decltype(SL)::value;
+    const int pin = c.pin0 + i * c.dpin;
     const int j = i & 31;
     const int b = i >> 5;
     const float* tile = taps + (b & 1) * tile_stride;
@@ -132,9 +155,9 @@ __global__ void __launch_bounds__(32 * f16_block_warps<OCC>(), OCC) lbp_forward_
     float pm = kInf;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
-      const float cst = __half2float(ncst[kk]);
-      const float va = __half2float(nva[kk]);
-      const float vb = __half2float(nvb[kk]);
+      const float cst = __half2float(pcst[sl][kk]);
+      const float va = __half2float(pva[sl][kk]);
+      const float vb = __half2float(pvb[sl][kk]);
       const float hv = (a.phase == 0) ? ((cst + chain[kk]) + va) + vb : ((cst + va) + vb) + chain[kk];
       h[kk] = lvalid(kk) ? hv : kInf;
       hs[lane + 32 * kk] = h[kk];
@@ -149,7 +172,7 @@ __global__ void __launch_bounds__(32 * f16_block_warps<OCC>(), OCC) lbp_forward_
       argmin_h = __reduce_max_sync(FULL, ll);
     }
     __syncwarp();  // h of the whole pixel is visible in hs
-    if (i + 1 < nsteps) prefetch(i + 1);
+    if (i + PF < nsteps) prefetch(SL, i + PF);
 
     const float w = tile[a.Lv * 33 + j];
     float msg[K];
@@ -303,6 +326,13 @@ __global__ void __launch_bounds__(32 * f16_block_warps<OCC>(), OCC) lbp_forward_
       }
     }
     __syncwarp();  // hs is rewritten by the next step
+  };
+  for (int i0 = 0; i0 < nsteps; i0 += PF) {
+    static_for<PF>([&](auto SL) {
+      constexpr int s = decltype(SL)::value;
+      const int i = i0 + s;
+      if (i < nsteps) step(SL, i);
+    });
   }
 }
 
@@ -313,10 +343,10 @@ constexpr int kF16HiOcc = 17;
 
 template <int K, bool SCALE>
 int launch_f16_phase(const FwdArgs& a, cudaStream_t stream) {
-  auto kern = lbp_forward_f16_kernel<K, 1, SCALE>;
+  auto kern = lbp_forward_f16_kernel<K, 1, SCALE, 3>;
   int wpb = 4;
   if (a.nchains > kHiOccChainsPerSm * sm_count()) {
-    kern = lbp_forward_f16_kernel<K, kF16HiOcc, SCALE>;
+    kern = lbp_forward_f16_kernel<K, kF16HiOcc, SCALE, 1>;
     wpb = 1;
   }
   const size_t per_warp = 4 * static_cast<size_t>(align4(32 * K + 2 * kHsPad) + 2 * tap_tile_rows(a.Lv) * 33);

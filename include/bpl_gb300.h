@@ -299,6 +299,25 @@ int bpl_messages_argmin(const void* messages, int messages_half, const void* cos
 int bpl_beliefs_infer(const float* beliefs, int mode, int support, void* out, int B, int H, int W, int L,
                       void* stream);
 
+/*
+ * Stereo jump taps from per-pixel affinities, in one pass
+ * (LBPMinSumFunction.forward, ops/lbp_stereo/message_passing_op_cuda.py:35-60):
+ * affinities (N,4,K,H,W) [L2-, L2+, L1-, L1+, L3] (K = 5) or [L1, L1, L2]
+ * (K = 3) and offset (N,4,H,W) -> taps (N,4,K+3,H,W)
+ * [offset, L3, .., 0, .., L3], the pairs of directions RIGHT-to-LEFT and
+ * DOWN-to-UP in reverse order.  K odd, 3..13.
+ */
+int bpl_pack_taps(const float* affinities, const float* offset, float* taps, int N, int K, int H, int W,
+                  void* stream);
+
+/*
+ * Its gradient fold (message_passing_op_cuda.py:75-93): grad_affinities
+ * (N,4,K,H,W), each affinity the gradient of the taps it fills (L3: taps 1
+ * and K+2), and grad_offset (N,4,H,W) = tap 0's.
+ */
+int bpl_unpack_tap_grad(const float* grad_taps, float* grad_affinities, float* grad_offset, int N, int K, int H,
+                        int W, void* stream);
+
 /* Disparity count D of the SAD volume: (int)((max_disp - min_disp + 1) / step)
  * (ops/sad/src/stereo_sad_kernel.cu:122); -1 for a non-positive step. */
 int bpl_sad_volume_depth(int min_disp, int max_disp, float step);

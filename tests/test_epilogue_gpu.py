@@ -77,3 +77,53 @@ def test_beliefs_infer_matches_the_reference_modes(L):
     # the layer routes both modes through the kernel without a gradient
     assert torch.equal(Inference(dev(), "wta")(beliefs), torch.argmax(beliefs, dim=3, keepdim=True))
     assert (Inference(dev(), "sub-exp")(beliefs) - want).abs().max().item() <= 1e-5 * max(1.0, L)
+
+
+def _pack_torch(aff, off):
+    # the reference's packing statement (message_passing_op_cuda.py:35-60)
+    N, D, K, H, W = aff.shape
+    out = torch.zeros((N, D, K + 3, H, W), device=aff.device)
+    out[:, :, 0] = off
+    out[:, :, 1] = aff[:, :, -1]
+    out[:, :, -1] = aff[:, :, -1]
+    ic = 0
+    for i in range(2, (K + 3) // 2):
+        out[:, 0::2, i] = aff[:, 0::2, ic]
+        out[:, 0::2, -i] = aff[:, 0::2, ic + 1]
+        out[:, 1::2, i] = aff[:, 1::2, ic + 1]
+        out[:, 1::2, -i] = aff[:, 1::2, ic]
+        ic += 2
+    return out
+
+
+def _unpack_torch(gt):
+    # the reference's fold (message_passing_op_cuda.py:75-93)
+    N, D, Kp, H, W = gt.shape
+    g = torch.zeros((N, D, Kp - 3, H, W), device=gt.device)
+    g[:, :, -1] += gt[:, :, 1]
+    g[:, :, -1] += gt[:, :, -1]
+    ic = 0
+    for i in range(2, Kp // 2):
+        g[:, 0::2, ic] = gt[:, 0::2, i]
+        g[:, 0::2, ic + 1] = gt[:, 0::2, -i]
+        g[:, 1::2, ic + 1] = gt[:, 1::2, i]
+        g[:, 1::2, ic] = gt[:, 1::2, -i]
+        ic += 2
+    return g, gt[:, :, 0]
+
+
+@pytest.mark.parametrize("K", [3, 5])
+def test_tap_packing_kernels_match_the_reference_statements(K):
+    """bpl_pack_taps / bpl_unpack_tap_grad against the reference's packing and
+    fold statements: bit-identical (copies, and the L3 fold's two adds in the
+    same order)."""
+    from bpl_gb300 import ops
+    g = gen(K)
+    N, H, W = 2, 13, 21
+    aff = torch.rand((N, 4, K, H, W), device=dev(), generator=g)
+    off = torch.randn((N, 4, H, W), device=dev(), generator=g)
+    assert torch.equal(ops.pack_taps(aff, off), _pack_torch(aff, off))
+    gt = torch.randn((N, 4, K + 3, H, W), device=dev(), generator=g)
+    ga, go = ops.unpack_tap_grad(gt)
+    ra, ro = _unpack_torch(gt)
+    assert torch.equal(ga, ra) and torch.equal(go, ro)
