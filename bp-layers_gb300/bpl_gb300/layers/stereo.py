@@ -57,8 +57,7 @@ class BeliefsSoftmin(torch.autograd.Function):
         B, _, H, W, Ls = messages.shape
         L = cost.shape[-1]
         if messages.dtype == torch.float16:
-            g1 = torch.zeros((B, 1, H, W, Ls), dtype=torch.float16, device=gz.device)
-            g1[:, 0, ..., :L] = gz
+            g1 = ops.to_half_padded(gz, L).unsqueeze(1)
         else:
             g1 = gz.unsqueeze(1)
         gm = g1.expand(B, 4, H, W, Ls)
@@ -337,10 +336,12 @@ class MessagePassing(nn.Module):
         if self.storage == "fp16":
             cost_h = ops.to_half_padded(cost.detach(), C)
             if messages is None or messages.dtype != torch.float16:
+                # a half copy of the caller's start (or zeros): no gradient
+                # reaches the caller's float tensor through it, so none is kept
                 m = torch.zeros((N, 4, H, W, ops.padded_labels(C)), dtype=torch.float16, device=dev)
                 if messages is not None:
                     m[..., :C] = messages.detach()
-                messages = m.requires_grad_(True)
+                messages = m
             messages = LBPMinSumLoop.apply(cost, cost_h, edge_weights, messages, self.delta, affinities, offset,
                                            self.max_iter, "reference", self.recompute_argmin)
             return BeliefsSoftmin.apply(messages, cost, self.softmin.T), messages

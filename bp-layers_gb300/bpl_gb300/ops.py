@@ -304,8 +304,11 @@ def padded_labels(L: int) -> int:
 
 
 def to_half_padded(t: torch.Tensor, L: int) -> torch.Tensor:
-    """Copy a (..., L) tensor into a zero-padded (..., Lp) half tensor."""
+    """Copy a (..., L) tensor into a zero-padded (..., Lp) half tensor (one
+    conversion pass when L is already a multiple of 8)."""
     Lp = padded_labels(L)
+    if Lp == L and t.shape[-1] == L:
+        return t.to(torch.float16).contiguous()
     out = torch.zeros(tuple(t.shape[:-1]) + (Lp,), dtype=torch.float16, device=t.device)
     out[..., :L] = t
     return out

@@ -276,31 +276,33 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
   const int trow = a.Lv + 2;
   // Loaded 32 steps ahead and written to the tile when its block starts; the
   // registers are not read before then, so the loads never stall a step.
-  // Constant register indices (a run-time index would put rg on the stack).
+  // Constant register indices (a run-time index would put rg on the stack);
+  // NR of them, the tap count when it is a compile-time constant.
+  constexpr int NR = (LV == 6 || LV == 8) ? LV : 16;
   float ev = 0.0f;
-  auto load_tile_regs = [&](int b, float (&rg)[16]) {
+  auto load_tile_regs = [&](int b, float (&rg)[NR]) {
     const int k = min(32 * b + lane, nsteps - 1);  // lanes past the end reload the last step
     const int p = pin0 + k * dpin;
     ev = __ldg(edge_fd + p);
     if (stereo) {
 #pragma unroll
-      for (int j = 0; j < 16; ++j)
-        if (j < a.Lv) rg[j] = __ldg(jump_fd + static_cast<int64_t>(j) * HW + p);
+      for (int j = 0; j < NR; ++j)
+        if (NR == LV || j < a.Lv) rg[j] = __ldg(jump_fd + static_cast<int64_t>(j) * HW + p);
     }
   };
-  auto store_tile = [&](float* tile, const float (&rg)[16]) {
+  auto store_tile = [&](float* tile, const float (&rg)[NR]) {
     if (stereo) {
 #pragma unroll
-      for (int j = 0; j < 16; ++j)
-        if (j < a.Lv) tile[j * 33 + lane] = rg[j];
+      for (int j = 0; j < NR; ++j)
+        if (NR == LV || j < a.Lv) tile[j * 33 + lane] = rg[j];
     }
     tile[a.Lv * 33 + lane] = ev;
   };
 
   prefetch(0);
-  float rg[16];
+  float rg[NR];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) rg[j] = 0.0f;
+  for (int j = 0; j < NR; ++j) rg[j] = 0.0f;
   load_tile_regs(0, rg);
   store_tile(sm.tile, rg);
   if (nsteps > 32) load_tile_regs(1, rg);
@@ -343,9 +345,9 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
     }
     if (k + 1 < nsteps) prefetch(k + 1);
 
-    // both sums in one reduce-scatter: lanes < 16 end with sum(g), the
-    // others with sum(accH)
-    {
+    if (sizeof(T) == 4) {
+      // both sums in one reduce-scatter: lanes < 16 end with sum(g), the
+      // others with sum(accH)
       float v = (lane & 16) ? sa : sg;
       const float o = __shfl_xor_sync(FULL, (lane & 16) ? sg : sa, 16);
       v += o;
@@ -353,12 +355,19 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
       for (int o2 = 8; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(FULL, v, o2);
       sg = __shfl_sync(FULL, v, 0);
       sa = __shfl_sync(FULL, v, 16);
-    }
-    if (sizeof(T) == 2) {
-      // p = exp(row) / se: scale the two sums instead of every p
-      const float inv_s = 1.0f / warp_sum(se);
-      sg *= inv_s;
-      sa *= inv_s;
+    } else {
+      // three sums in one reduce-scatter: lanes 0-7 end with sum(g), 8-15
+      // with sum(accH), 16-23 with sum(exp(row)); p = exp(row) / se, so the
+      // two sums are scaled instead of every p
+      const bool h16 = lane & 16, h8 = lane & 8;
+      const float w0 = (h16 ? se : sg) + __shfl_xor_sync(FULL, h16 ? sg : se, 16);
+      const float w1 = (h16 ? 0.0f : sa) + __shfl_xor_sync(FULL, h16 ? sa : 0.0f, 16);
+      float v = (h8 ? w1 : w0) + __shfl_xor_sync(FULL, h8 ? w0 : w1, 8);
+#pragma unroll
+      for (int o2 = 4; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(FULL, v, o2);
+      const float inv_s = 1.0f / __shfl_sync(FULL, v, 16);
+      sg = __shfl_sync(FULL, v, 0) * inv_s;
+      sa = __shfl_sync(FULL, v, 8) * inv_s;
     }
     float addH[K], addU[K], addD[K];
 #pragma unroll
