@@ -1,7 +1,7 @@
 """Builds libbpl_gb300.so (the C-ABI library with all CUDA kernels) in-tree.
 
 nvcc compiles each translation unit of csrc/ for sm_103a in parallel, then
-links them (with device linking, the units share device symbols) into
+links them (with device linking for the units that share device symbols) into
 bp-layers_gb300/_build/libbpl_gb300.so.  No torch headers are involved, so
 the build is a few nvcc calls.
 """
@@ -26,6 +26,19 @@ NVCC_FLAGS = [
     "-std=c++17", "-O3", "-lineinfo", f"-gencode=arch=compute_{ARCH},code=sm_{ARCH}",
     "-rdc=true", "-Xcompiler", "-fPIC", "--fmad=false", "-Xptxas", "-warn-spills",
 ]
+# Units that reference no device symbol of another unit (the device error
+# word and the wait limit are declared for relocatable units only, so such a
+# reference does not compile) are compiled as whole programs: relocatable code
+# gave the adjoint kernels a stack frame (local loads on every step) that
+# whole-program code does not have.  They link beside the relocatable units;
+# only the latter take part in device linking.
+WHOLE_PROGRAM_PREFIXES = ("lbp_backward", "sad.cu", "beliefs.cu", "epilogue.cu", "pyramid.cu")
+
+
+def _flags(src: str):
+    if os.path.basename(src).startswith(WHOLE_PROGRAM_PREFIXES):
+        return [f if f != "-rdc=true" else "-rdc=false" for f in NVCC_FLAGS]
+    return NVCC_FLAGS
 
 
 def _nvcc() -> str:
@@ -43,7 +56,7 @@ def _deps_digest() -> str:
         with open(f, "rb") as fh:
             h.update(os.path.basename(f).encode())
             h.update(fh.read())
-    h.update(" ".join(NVCC_FLAGS).encode())
+    h.update(" ".join(NVCC_FLAGS + list(WHOLE_PROGRAM_PREFIXES)).encode())
     return h.hexdigest()
 
 
@@ -62,7 +75,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for src in _sources():
         obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
         objs.append(obj)
-        cmds.append([nvcc, "-c", src, "-o", obj, "-I", INCLUDE] + NVCC_FLAGS)
+        cmds.append([nvcc, "-c", src, "-o", obj, "-I", INCLUDE] + _flags(src))
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -27,11 +27,16 @@ __host__ __device__ constexpr int np2(int k) {
 }
 
 // Error word written by kernels whose bounded waits ran out.  Read with
-// bpl_read_device_error().
+// bpl_read_device_error().  Declared for relocatable units only (the ones
+// device-linked with its definition): a unit compiled as a whole program
+// that used it would get a private copy the library never reads, so there
+// it does not compile.
+#ifdef __CUDACC_RDC__
 extern __device__ int g_bpl_error;
 // Poll limit of the bounded waits (default kWaitLimit; bpl_set_wait_limit
 // lowers it so that a test can make a wait run out).
 extern __device__ unsigned g_bpl_wait_limit;
+#endif
 constexpr unsigned kWaitLimit = 1u << 24;
 // Poll limit of the drain that waits for a failed kernel's copies in flight
 // (independent of g_bpl_wait_limit: those copies always land).
@@ -39,7 +44,9 @@ constexpr unsigned kDrainLimit = 1u << 20;
 
 enum DeviceError { DEV_ERR_NONE = 0, DEV_ERR_WAIT_TIMEOUT = 1 };
 
+#ifdef __CUDACC_RDC__
 __device__ __forceinline__ void raise_device_error(int code) { atomicCAS(&g_bpl_error, 0, code); }
+#endif
 
 // ---------------------------------------------------------------------------
 // Warp reductions with the reference's tree order.
@@ -200,6 +207,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+#ifdef __CUDACC_RDC__
 // Bounded wait: gives up after `limit` polls (each poll may suspend for a
 // hardware-defined interval), raising DEV_ERR_WAIT_TIMEOUT.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
@@ -212,6 +220,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
   return mbar_wait_bounded(bar, parity, *static_cast<volatile unsigned*>(&g_bpl_wait_limit));
 }
+#endif
 
 // 4-byte cp.async (any alignment) with group commit/wait, for rows whose
 // length is not a multiple of 16 bytes.
