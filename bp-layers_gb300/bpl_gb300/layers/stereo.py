@@ -266,6 +266,83 @@ class LBPMinSumLoop(torch.autograd.Function):
         return gc, gtaps, ge, in_grad
 
 
+class BPLayerFn(torch.autograd.Function):
+    """MessagePassing's passes and belief epilogue as one autograd node
+    (reference adjoint, argmin indices stored), FP32 or FP16 storage.
+
+    forward(prob_vol, edge, messages, affinities, offset, T, iters, delta)
+    -> (beliefs, messages): cost = -prob_vol (message_passing_op_cuda.py:
+    162), `iters` passes in place on messages (FP16: (N,4,H,W,Lp) half, the
+    cost volume the half copy of -prob_vol), beliefs = softmin((sum + cost)
+    / T) (:170-173, read from prob_vol with the sign folded in).  Values and
+    gradients are those of the composition LBPMinSumLoop + BeliefsSoftmin
+    (which the other modes run; the cost gradient up to the order of its
+    float additions).  What the single node saves: the beliefs' backward
+    writes its cost gradient negated into the buffer that becomes the
+    probability volume's gradient, and the adjoint adds its own there with
+    sign -1, so autograd's sum of the cost's two gradients and the
+    negation's backward take no pass and the adjoint no zero-fill; the
+    beliefs' backward also writes the adjoint's in_grad (for a leaf message
+    tensor the materialised message gradient) in the same pass."""
+
+    @staticmethod
+    def forward(ctx, prob_vol, edge, messages, affinities, offset, T, iters, delta):
+        ctx.set_materialize_grads(False)
+        taps = pack_affinities(affinities, offset)
+        half = messages.dtype == torch.float16
+        prob = prob_vol.contiguous()
+        B, H, W, L = prob.shape
+        Ls = messages.shape[-1]
+        am_dtype = torch.uint8 if L <= 256 else torch.int16
+        cost = ops.half_padded(prob, -1.0) if half else -prob
+        argmins = torch.empty((iters, B, 4, H, W, Ls), dtype=am_dtype, device=prob.device)
+        # FP16: no scales (the adjoint normalises from the final rows)
+        scales = None if half else torch.empty((iters, B, 4, H, W), dtype=torch.float32, device=prob.device)
+        for k in range(iters):
+            if half:
+                ops.lbp_forward_f16(ops.LBP_STEREO, cost, taps, edge, messages, int(delta), L,
+                                    argmin_dtype=am_dtype, argmin=argmins[k])
+            else:
+                ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta), argmin_dtype=am_dtype,
+                                argmin=argmins[k], scale=scales[k])
+        beliefs = ops.beliefs_forward_any_cost(messages, prob, T, L, cost_sign=-1.0)
+        ctx.save_for_backward(prob, taps, edge, messages, argmins, scales, T, beliefs)
+        ctx.half, ctx.L = half, L
+        ctx.leaf_messages = messages.is_leaf
+        return beliefs, messages
+
+    @staticmethod
+    def backward(ctx, grad_beliefs, grad_messages):
+        prob, taps, edge, messages, argmins, scales, T, beliefs = ctx.saved_tensors
+        B, _, H, W, Ls = messages.shape
+        need_m = ctx.needs_input_grad[2]
+        if grad_beliefs is None:
+            grad_beliefs = torch.zeros_like(beliefs)
+        if ctx.half:
+            kind = ops.BELIEF_COPY_HALF
+        elif need_m and grad_messages is None:
+            kind = ops.BELIEF_COPY_SLOTS
+        else:
+            kind = ops.BELIEF_COPY_FLOAT
+        gprob, gcopy, gT = ops.beliefs_backward_fused(messages, prob, T, beliefs, grad_beliefs, -1.0, kind,
+                                                      want_temperature=ctx.needs_input_grad[5], cost_sign=-1.0)
+        if grad_messages is not None:
+            # the returned messages are used downstream too: their gradient
+            # joins the beliefs' in every slot
+            gin = (gcopy.float() + grad_messages.float()).to(messages.dtype).contiguous()
+        elif kind == ops.BELIEF_COPY_SLOTS:
+            gin = gcopy
+        else:
+            gin = gcopy.expand(B, 4, H, W, gcopy.shape[-1])
+        _, gtaps, ge = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, gin, messages, argmins, scales, L=ctx.L,
+                                               grad_cost_into=gprob, cost_sign=-1.0)
+        g_aff, g_off = unpack_affinity_grad(gtaps)
+        gm = None
+        if need_m:
+            gm = ops.leaf_message_grad(gin) if ctx.leaf_messages else gin
+        return gprob, ge, gm, g_aff, g_off, (gT.view_as(T) if gT is not None else None), None, None
+
+
 class MessagePassing(nn.Module):
     """message_passing_op_cuda.py:95-177.  storage="fp16" keeps the cost
     volume and the messages in half precision (label axis padded to a
@@ -292,8 +369,12 @@ class MessagePassing(nn.Module):
             raise ValueError("L1 must be smaller than or equal L2!")
 
     def __init__(self, device, max_iter, num_labels, delta, mode="min-sum", storage="fp32", adjoint="reference",
-                 recompute_argmin=False):
+                 recompute_argmin=False, fused=True):
         super().__init__()
+        # fused: the reference adjoint with stored indices runs as one autograd
+        # node (BPLayerFn); False keeps the composition of LBPMinSumLoop and
+        # BeliefsSoftmin (the same values)
+        self.fused = fused
         self.device = device
         self.max_iter = max_iter
         if mode != "min-sum":
@@ -332,9 +413,11 @@ class MessagePassing(nn.Module):
                 raise ValueError("L1 or L2 is None and affinities are not set!")
         if offset is None:
             offset = torch.zeros((N, 4, H, W), device=dev)
-        cost = -prob_vol
+        fused = self.fused and self.adjoint == "reference" and not self.recompute_argmin and self.max_iter >= 1
+        if fused and self.storage == "fp32":
+            return BPLayerFn.apply(prob_vol, edge_weights, messages, affinities, offset, self.softmin.T,
+                                   self.max_iter, self.delta)
         if self.storage == "fp16":
-            cost_h = ops.to_half_padded(cost.detach(), C)
             if messages is None or messages.dtype != torch.float16:
                 # a half copy of the caller's start (or zeros): no gradient
                 # reaches the caller's float tensor through it, so none is kept
@@ -342,9 +425,15 @@ class MessagePassing(nn.Module):
                 if messages is not None:
                     m[..., :C] = messages.detach()
                 messages = m
+            if fused:
+                return BPLayerFn.apply(prob_vol, edge_weights, messages, affinities, offset, self.softmin.T,
+                                       self.max_iter, self.delta)
+            cost = -prob_vol
+            cost_h = ops.to_half_padded(cost.detach(), C)
             messages = LBPMinSumLoop.apply(cost, cost_h, edge_weights, messages, self.delta, affinities, offset,
                                            self.max_iter, "reference", self.recompute_argmin)
             return BeliefsSoftmin.apply(messages, cost, self.softmin.T), messages
+        cost = -prob_vol
         if self.adjoint == "reference" or self.recompute_argmin:
             messages = LBPMinSumLoop.apply(cost, None, edge_weights, messages, self.delta, affinities, offset,
                                            self.max_iter, self.adjoint, self.recompute_argmin)

@@ -421,7 +421,8 @@ def lbp_backward_f16(variant: int, jump, edge: torch.Tensor, in_grad_h: torch.Te
 
 def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.Tensor, messages: torch.Tensor,
                         argmins: torch.Tensor, scales: torch.Tensor, L: int | None = None,
-                        workspace: torch.Tensor | None = None):
+                        workspace: torch.Tensor | None = None, grad_cost_into: torch.Tensor | None = None,
+                        cost_sign: float = 1.0):
     """Reference adjoint of P passes run in place on one messages tensor,
     in one launch: argmins (P,B,4,H,W,Ls) and scales (P,B,4,H,W) stacked in
     pass order; in_grad and messages shared (the reference's backward of each
@@ -429,7 +430,11 @@ def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.T
     (messages float32) or FP16 storage (messages half, padded label axis,
     L given; scales may be None, the FP16 adjoint normalising from the
     rows).  Returns (grad_cost, grad_jump, grad_edge) summed over the
-    passes; the message gradient is in_grad."""
+    passes; the message gradient is in_grad.
+
+    grad_cost_into: a float (B,H,W,L) or (B,H,W,Ls) tensor the cost
+    gradient is added onto, times cost_sign (+1 or -1), instead of a new
+    zeroed one (bpl_lbp_backward_passes_into); it is returned as grad_cost."""
     half = messages.dtype == torch.float16
     if not isinstance(in_grad, torch.Tensor) or in_grad.dtype != messages.dtype or in_grad.dim() != 5 \
             or not in_grad.is_cuda:
@@ -472,17 +477,31 @@ def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.T
         grad_jump = torch.empty((B, 4, L, L), dtype=torch.float32, device=dev)
     else:
         grad_jump = torch.empty((_pixel_planes(variant), H, W, L, L), dtype=torch.float32, device=dev)
-    grad_cost = torch.empty((B, H, W, Ls), dtype=torch.float32, device=dev)
     grad_edge = None if _pixel(variant) else torch.empty(tuple(edge.shape), dtype=torch.float32, device=dev)
     need = P * lbp_backward_workspace_bytes(B, H, W, Ls)
     if workspace is None or workspace.numel() * workspace.element_size() < need:
         workspace = torch.empty(need, dtype=torch.uint8, device=dev)
-    fn = lib().bpl_lbp_backward_passes_f16 if half else lib().bpl_lbp_backward_passes
     name = "lbp_backward_f16" if half else "lbp_backward"
-    st = _timed(name, lambda: fn(
-        variant, _ptr(jump) if not _pixel(variant) else None, _ptr(edge), _ptr(in_grad), g_bstride, g_sstride,
-        _ptr(messages), _ptr(argmins), kind, _ptr(scales), _ptr(grad_cost), _ptr(grad_jump), _ptr(grad_edge), _ptr(workspace),
-        workspace.numel() * workspace.element_size(), B, H, W, L, Lv, jb, edge.shape[0], P, _stream(messages)))
+    ws_bytes = workspace.numel() * workspace.element_size()
+    jp = _ptr(jump) if not _pixel(variant) else None
+    if grad_cost_into is None:
+        grad_cost = torch.empty((B, H, W, Ls), dtype=torch.float32, device=dev)
+        fn = lib().bpl_lbp_backward_passes_f16 if half else lib().bpl_lbp_backward_passes
+        st = _timed(name, lambda: fn(
+            variant, jp, _ptr(edge), _ptr(in_grad), g_bstride, g_sstride, _ptr(messages), _ptr(argmins), kind,
+            _ptr(scales), _ptr(grad_cost), _ptr(grad_jump), _ptr(grad_edge), _ptr(workspace), ws_bytes, B, H, W, L,
+            Lv, jb, edge.shape[0], P, _stream(messages)))
+    else:
+        grad_cost = grad_cost_into
+        _check_input("grad_cost_into", grad_cost, dim=4)
+        if tuple(grad_cost.shape[:3]) != (B, H, W) or grad_cost.shape[3] not in (L, Ls):
+            raise BplError("grad_cost_into must be (B,H,W,L) or (B,H,W,Ls)")
+        if cost_sign not in (1.0, -1.0):
+            raise BplError("cost_sign must be +1 or -1")
+        st = _timed(name, lambda: lib().bpl_lbp_backward_passes_into(
+            int(half), variant, jp, _ptr(edge), _ptr(in_grad), g_bstride, g_sstride, _ptr(messages), _ptr(argmins),
+            kind, _ptr(scales), _ptr(grad_cost), grad_cost.shape[3], float(cost_sign), _ptr(grad_jump),
+            _ptr(grad_edge), _ptr(workspace), ws_bytes, B, H, W, L, Lv, jb, edge.shape[0], P, _stream(messages)))
     check(st, "bpl_lbp_backward_passes")
     return grad_cost, grad_jump, grad_edge
 
@@ -543,6 +562,75 @@ def leaf_message_grad(in_grad: torch.Tensor) -> torch.Tensor:
         if src.is_contiguous():
             return broadcast_slots(src)
     return in_grad
+
+
+def half_padded(src: torch.Tensor, sign: float = 1.0) -> torch.Tensor:
+    """(..., L) float -> (..., Lp) half of sign * src, labels L..Lp-1 zeroed,
+    one kernel pass (bpl_half_padded); the FP16-storage cost volume from the
+    probability volume with sign -1."""
+    _check_input("src", src, dim=None)
+    L = src.shape[-1]
+    Lp = padded_labels(L)
+    out = torch.empty(tuple(src.shape[:-1]) + (Lp,), dtype=torch.float16, device=src.device)
+    rows = src.numel() // L
+    st = _timed("half_padded", lambda: lib().bpl_half_padded(_ptr(src), float(sign), _ptr(out), rows, L, Lp,
+                                                             _stream(src)))
+    check(st, "bpl_half_padded")
+    return out
+
+
+def beliefs_forward_any_cost(messages: torch.Tensor, cost: torch.Tensor, temperature: torch.Tensor, L: int,
+                             out: torch.Tensor | None = None, cost_sign: float = 1.0) -> torch.Tensor:
+    """beliefs_forward with z = sum + cost_sign * cost, the cost float
+    (B,H,W,L) or the FP16-storage half volume (B,H,W,Lp)
+    (bpl_beliefs_forward_ex); cost_sign -1 takes the probability volume."""
+    _check_input("messages", messages, dtype=None, dim=5)
+    _check_input("cost", cost, dtype=None, dim=4)
+    B, _, H, W, Ls = messages.shape
+    if out is None:
+        out = torch.empty((B, H, W, L), dtype=torch.float32, device=cost.device)
+    st = _timed("beliefs_forward", lambda: lib().bpl_beliefs_forward_ex(
+        _ptr(messages), int(messages.dtype == torch.float16), _ptr(cost), int(cost.dtype == torch.float16),
+        float(cost_sign), _ptr(temperature), _ptr(out), B, H, W, L, Ls, _stream(cost)))
+    check(st, "bpl_beliefs_forward_ex")
+    return out
+
+
+BELIEF_COPY_NONE, BELIEF_COPY_HALF, BELIEF_COPY_SLOTS, BELIEF_COPY_FLOAT = 0, 1, 2, 3
+
+
+def beliefs_backward_fused(messages: torch.Tensor, cost: torch.Tensor, temperature: torch.Tensor,
+                           beliefs: torch.Tensor, grad_beliefs: torch.Tensor, grad_z_sign: float, copy_kind: int,
+                           want_temperature: bool = True, cost_sign: float = 1.0):
+    """Gradient of the fused epilogue for the layer's fused backward
+    (bpl_beliefs_backward_ex): returns (grad_z_sign * grad_z (B,H,W,L),
+    the copy of +grad_z selected by copy_kind or None, grad_T or None).
+    copy_kind: BELIEF_COPY_HALF (B,1,H,W,Lp) half, BELIEF_COPY_SLOTS
+    (B,4,H,W,L) float, BELIEF_COPY_FLOAT (B,1,H,W,L) float; cost and
+    cost_sign as beliefs_forward_any_cost."""
+    _check_input("beliefs", beliefs, dim=4)
+    grad_beliefs = grad_beliefs.contiguous()
+    _check_input("grad_beliefs", grad_beliefs, dim=4)
+    B, _, H, W, Ls = messages.shape
+    L = beliefs.shape[-1]
+    dev = beliefs.device
+    gz = torch.empty_like(beliefs)
+    if copy_kind == BELIEF_COPY_HALF:
+        copy = torch.empty((B, 1, H, W, padded_labels(L)), dtype=torch.float16, device=dev)
+    elif copy_kind == BELIEF_COPY_SLOTS:
+        copy = torch.empty((B, 4, H, W, L), dtype=torch.float32, device=dev)
+    elif copy_kind == BELIEF_COPY_FLOAT:
+        copy = torch.empty((B, 1, H, W, L), dtype=torch.float32, device=dev)
+    else:
+        copy = None
+    gT = torch.empty(1, dtype=torch.float32, device=dev) if want_temperature else None
+    st = _timed("beliefs_backward", lambda: lib().bpl_beliefs_backward_ex(
+        _ptr(messages), int(messages.dtype == torch.float16), _ptr(cost), int(cost.dtype == torch.float16),
+        float(cost_sign), _ptr(temperature), _ptr(beliefs), _ptr(grad_beliefs), _ptr(gz), float(grad_z_sign),
+        _ptr(copy), copy_kind,
+        _ptr(gT), B, H, W, L, Ls, _stream(beliefs)))
+    check(st, "bpl_beliefs_backward_ex")
+    return gz, copy, gT
 
 
 def beliefs_backward(messages: torch.Tensor, cost: torch.Tensor, temperature: torch.Tensor, beliefs: torch.Tensor,

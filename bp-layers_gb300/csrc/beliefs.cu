@@ -35,28 +35,31 @@ __device__ __forceinline__ float warp_max(float v) {
 }
 
 // z / T for the labels of one pixel (K per lane); invalid labels -> +inf.
-template <int K, typename T>
-__device__ __forceinline__ void load_z(const T* msgs, const float* cost, int64_t pix, int64_t HWLs, int Ls, int L,
-                                       int n, int64_t HW, float Tm, int lane, float (&zt)[K]) {
+// The cost is float (label stride L) or the FP16-storage half volume (label
+// stride Ls), taken times csign (+1; -1 reads the probability volume the
+// layer's cost is the negation of, exactly: negation is exact).
+template <int K, typename T, typename TC>
+__device__ __forceinline__ void load_z(const T* msgs, const TC* cost, float csign, int64_t pix, int64_t HWLs, int Ls,
+                                       int L, int n, int64_t HW, float Tm, int lane, float (&zt)[K]) {
   const int64_t p = pix % HW;
   const T* m = msgs + (static_cast<int64_t>(n) * 4) * HWLs + p * Ls;
-  const float* c = cost + pix * L;
+  const TC* c = cost + pix * (sizeof(TC) == 4 ? L : Ls);
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     const int t = lane + 32 * k;
     if (t < L) {
       const float s = __fadd_rn(__fadd_rn(__fadd_rn(tof<T>(m[t]), tof<T>(m[HWLs + t])), tof<T>(m[2 * HWLs + t])),
                                 tof<T>(m[3 * HWLs + t]));
-      zt[k] = __fdiv_rn(__fadd_rn(s, c[t]), Tm);
+      zt[k] = __fdiv_rn(__fadd_rn(s, csign * tof<TC>(c[t])), Tm);
     } else {
       zt[k] = __int_as_float(0x7f800000);
     }
   }
 }
 
-template <int K, typename T>
-__global__ void __launch_bounds__(256) beliefs_fwd_kernel(const T* msgs, const float* cost, const float* Tp, float* out,
-                                                          int B, int H, int W, int L, int Ls) {
+template <int K, typename T, typename TC>
+__global__ void __launch_bounds__(256) beliefs_fwd_kernel(const T* msgs, const TC* cost, float csign, const float* Tp,
+                                                          float* out, int B, int H, int W, int L, int Ls) {
   const int lane = threadIdx.x & 31;
   const int64_t HW = static_cast<int64_t>(H) * W;
   const int64_t npix = B * HW;
@@ -67,7 +70,7 @@ __global__ void __launch_bounds__(256) beliefs_fwd_kernel(const T* msgs, const f
        pix += warps) {
     const int n = static_cast<int>(pix / HW);
     float zt[K];
-    load_z<K, T>(msgs, cost, pix, HWLs, Ls, L, n, HW, Tm, lane, zt);
+    load_z<K, T, TC>(msgs, cost, csign, pix, HWLs, Ls, L, n, HW, Tm, lane, zt);
     // softmin(x) = softmax(-x): shift by the minimum of x
     float mn = zt[0];
 #pragma unroll
@@ -88,10 +91,17 @@ __global__ void __launch_bounds__(256) beliefs_fwd_kernel(const T* msgs, const f
   }
 }
 
-template <int K, typename T>
-__global__ void __launch_bounds__(256) beliefs_bwd_kernel(const T* msgs, const float* cost, const float* Tp,
-                                                          const float* y, const float* gy, float* gz, float* gT,
-                                                          int B, int H, int W, int L, int Ls) {
+// Gradient outputs: gz (B,H,W,L) float receives gz_sign * dL/dz; `copy`, by
+// copy_kind, a second copy of +dL/dz: kCopyHalf (B,H,W,Ls) half with the
+// padding zeroed, kCopySlots (B,4,H,W,L) float in every message slot,
+// kCopyFloat (B,H,W,L) float.
+enum { kCopyNone = 0, kCopyHalf = 1, kCopySlots = 2, kCopyFloat = 3 };
+
+template <int K, typename T, typename TC>
+__global__ void __launch_bounds__(256) beliefs_bwd_kernel(const T* msgs, const TC* cost, float csign, const float* Tp,
+                                                          const float* y, const float* gy, float* gz, float gz_sign,
+                                                          void* copy, int copy_kind, float* gT, int B, int H, int W,
+                                                          int L, int Ls) {
   const int lane = threadIdx.x & 31;
   const int64_t HW = static_cast<int64_t>(H) * W;
   const int64_t npix = B * HW;
@@ -103,7 +113,7 @@ __global__ void __launch_bounds__(256) beliefs_bwd_kernel(const T* msgs, const f
        pix += warps) {
     const int n = static_cast<int>(pix / HW);
     float zt[K];
-    if (gT != nullptr) load_z<K, T>(msgs, cost, pix, HWLs, Ls, L, n, HW, Tm, lane, zt);
+    if (gT != nullptr) load_z<K, T, TC>(msgs, cost, csign, pix, HWLs, Ls, L, n, HW, Tm, lane, zt);
     const float* yp = y + pix * L;
     const float* gp = gy + pix * L;
     float yv[K], gv[K], d = 0.0f;
@@ -116,15 +126,26 @@ __global__ void __launch_bounds__(256) beliefs_bwd_kernel(const T* msgs, const f
     }
     d = warp_sum(d);
     float* o = gz + pix * L;
+    const int64_t p = pix % HW;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       const int t = lane + 32 * k;
       // u = -z/T: du = y (g - sum(y g)); dz = -du / T; dT += du * z / T^2
       const float du = yv[k] * (gv[k] - d);
+      const float g = -du / Tm;
       if (t < L) {
-        o[t] = -du / Tm;
+        o[t] = gz_sign * g;
         if (gT != nullptr) tacc += du * (zt[k] / Tm);
+        if (copy_kind == kCopySlots) {
+          float* c = static_cast<float*>(copy) + static_cast<int64_t>(n) * 4 * HW * L + p * L + t;
+#pragma unroll
+          for (int sl = 0; sl < 4; ++sl) c[sl * HW * L] = g;
+        } else if (copy_kind == kCopyFloat) {
+          static_cast<float*>(copy)[pix * L + t] = g;
+        }
       }
+      if (copy_kind == kCopyHalf && t < Ls)
+        static_cast<__half*>(copy)[pix * Ls + t] = __float2half_rn(t < L ? g : 0.0f);
     }
   }
   if (gT != nullptr) {
@@ -138,12 +159,12 @@ int grid_for(int64_t npix) {
   return static_cast<int>(std::min<int64_t>(blocks, static_cast<int64_t>(sm_count()) * 16));
 }
 
-template <typename T>
-int fwd_impl(const T* msgs, const float* cost, const float* Tm, float* out, int B, int H, int W, int L, int Ls,
-             cudaStream_t s) {
+template <typename T, typename TC>
+int fwd_impl(const T* msgs, const TC* cost, const float* Tm, float* out, int B, int H, int W, int L, int Ls,
+             cudaStream_t s, float csign = 1.0f) {
   const int g = grid_for(static_cast<int64_t>(B) * H * W);
   const int k = (L + 31) / 32;
-#define BPL_BFWD(KK) beliefs_fwd_kernel<KK, T><<<g, 256, 0, s>>>(msgs, cost, Tm, out, B, H, W, L, Ls)
+#define BPL_BFWD(KK) beliefs_fwd_kernel<KK, T, TC><<<g, 256, 0, s>>>(msgs, cost, csign, Tm, out, B, H, W, L, Ls)
   if (k <= 1) BPL_BFWD(1);
   else if (k <= 2) BPL_BFWD(2);
   else if (k <= 4) BPL_BFWD(4);
@@ -156,13 +177,16 @@ int fwd_impl(const T* msgs, const float* cost, const float* Tm, float* out, int 
   return BPL_OK;
 }
 
-template <typename T>
-int bwd_impl(const T* msgs, const float* cost, const float* Tm, const float* y, const float* gy, float* gz, float* gT,
-             int B, int H, int W, int L, int Ls, cudaStream_t s) {
+template <typename T, typename TC>
+int bwd_impl(const T* msgs, const TC* cost, const float* Tm, const float* y, const float* gy, float* gz, float* gT,
+             int B, int H, int W, int L, int Ls, cudaStream_t s, float gz_sign = 1.0f, void* copy = nullptr,
+             int copy_kind = kCopyNone, float csign = 1.0f) {
   if (gT) BPL_CUDA_TRY(cudaMemsetAsync(gT, 0, sizeof(float), s), "beliefs_backward: memset");
   const int g = grid_for(static_cast<int64_t>(B) * H * W);
   const int k = (L + 31) / 32;
-#define BPL_BBWD(KK) beliefs_bwd_kernel<KK, T><<<g, 256, 0, s>>>(msgs, cost, Tm, y, gy, gz, gT, B, H, W, L, Ls)
+#define BPL_BBWD(KK)                                                                                  \
+  beliefs_bwd_kernel<KK, T, TC><<<g, 256, 0, s>>>(msgs, cost, csign, Tm, y, gy, gz, gz_sign, copy, copy_kind, gT, B, \
+                                                  H, W, L, Ls)
   if (k <= 1) BPL_BBWD(1);
   else if (k <= 2) BPL_BBWD(2);
   else if (k <= 4) BPL_BBWD(4);
@@ -234,6 +258,49 @@ extern "C" int bpl_beliefs_forward(const void* messages, int messages_half, cons
                     as_stream(stream));
   return fwd_impl(static_cast<const float*>(messages), cost, temperature, beliefs, B, H, W, L, Ls,
                   as_stream(stream));
+}
+
+extern "C" int bpl_beliefs_forward_ex(const void* messages, int messages_half, const void* cost, int cost_half,
+                                      float cost_sign, const float* temperature, float* beliefs, int B, int H, int W,
+                                      int L, int Ls, void* stream) {
+  BPL_TRACE("bpl_beliefs_forward_ex");
+  BPL_REQUIRE(messages && cost && beliefs && temperature, "beliefs_forward: null pointer");
+  BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1 && L >= 1 && L <= 1024 && Ls >= L, "beliefs_forward: bad shape");
+  BPL_REQUIRE(!cost_half || Ls == ((L + 7) & ~7), "beliefs_forward: a half cost has the padded label stride");
+  BPL_REQUIRE(cost_sign == 1.0f || cost_sign == -1.0f, "beliefs_forward: cost sign must be +-1");
+  cudaStream_t st = as_stream(stream);
+  const float cs = cost_sign;
+  if (messages_half) {
+    const __half* m = static_cast<const __half*>(messages);
+    return cost_half ? fwd_impl(m, static_cast<const __half*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs)
+                     : fwd_impl(m, static_cast<const float*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs);
+  }
+  const float* m = static_cast<const float*>(messages);
+  return cost_half ? fwd_impl(m, static_cast<const __half*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs)
+                   : fwd_impl(m, static_cast<const float*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs);
+}
+
+extern "C" int bpl_beliefs_backward_ex(const void* messages, int messages_half, const void* cost, int cost_half,
+                                       float cost_sign, const float* temperature, const float* beliefs, const float* grad_beliefs,
+                                       float* grad_z, float grad_z_sign, void* grad_copy, int copy_kind,
+                                       float* grad_temperature, int B, int H, int W, int L, int Ls, void* stream) {
+  BPL_TRACE("bpl_beliefs_backward_ex");
+  BPL_REQUIRE(beliefs && grad_beliefs && grad_z && temperature, "beliefs_backward: null pointer");
+  BPL_REQUIRE(grad_temperature == nullptr || (messages && cost), "beliefs_backward: null messages/cost");
+  BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1 && L >= 1 && L <= 1024 && Ls >= L, "beliefs_backward: bad shape");
+  BPL_REQUIRE(!cost_half || Ls == ((L + 7) & ~7), "beliefs_backward: a half cost has the padded label stride");
+  BPL_REQUIRE(grad_z_sign == 1.0f || grad_z_sign == -1.0f, "beliefs_backward: sign must be +-1");
+  BPL_REQUIRE(cost_sign == 1.0f || cost_sign == -1.0f, "beliefs_backward: cost sign must be +-1");
+  BPL_REQUIRE(copy_kind >= kCopyNone && copy_kind <= kCopyFloat, "beliefs_backward: bad copy kind %d", copy_kind);
+  BPL_REQUIRE(copy_kind == kCopyNone || grad_copy, "beliefs_backward: null gradient copy");
+  BPL_REQUIRE(copy_kind != kCopyHalf || Ls == ((L + 7) & ~7), "beliefs_backward: the half copy has stride Lp");
+  cudaStream_t st = as_stream(stream);
+#define BPL_BBWD_EX(MT, CT)                                                                                      \
+  bwd_impl(static_cast<const MT*>(messages), static_cast<const CT*>(cost), temperature, beliefs, grad_beliefs, \
+           grad_z, grad_temperature, B, H, W, L, Ls, st, grad_z_sign, grad_copy, copy_kind, cost_sign)
+  if (messages_half) return cost_half ? BPL_BBWD_EX(__half, __half) : BPL_BBWD_EX(__half, float);
+  return cost_half ? BPL_BBWD_EX(float, __half) : BPL_BBWD_EX(float, float);
+#undef BPL_BBWD_EX
 }
 
 extern "C" int bpl_beliefs_backward(const void* messages, int messages_half, const float* cost,

@@ -189,10 +189,42 @@ __global__ void unpack_tap_grad_kernel(const float* __restrict__ gtaps, float* _
   }
 }
 
+// dst (rows, Ls) half = sign * src (rows, L) float, padding labels zeroed:
+// the FP16-storage cost volume straight from the layer's probability volume
+// (cost = -prob), one pass.  One thread per label pair (Ls is even).
+__global__ void half_padded_kernel(const float* __restrict__ src, float sign, __half2* __restrict__ dst, int64_t rows,
+                                   int L, int Ls) {
+  const int hp = Ls / 2;
+  const int64_t total = rows * hp;
+  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < total;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = e / hp;
+    const int t = 2 * static_cast<int>(e % hp);
+    const float* s = src + r * L;
+    const float a = (t < L) ? sign * __ldg(s + t) : 0.0f;
+    const float b = (t + 1 < L) ? sign * __ldg(s + t + 1) : 0.0f;
+    dst[e] = __floats2half2_rn(a, b);
+  }
+}
+
 }  // namespace
 }  // namespace bpl
 
 using namespace bpl;
+
+extern "C" int bpl_half_padded(const float* src, float sign, void* dst, int64_t rows, int L, int Ls, void* stream) {
+  BPL_TRACE("bpl_half_padded");
+  BPL_REQUIRE(src && dst, "half_padded: null pointer");
+  BPL_REQUIRE(rows >= 1 && L >= 1 && Ls == ((L + 7) & ~7), "half_padded: bad shape (rows %lld, L %d, Ls %d)",
+              static_cast<long long>(rows), L, Ls);
+  BPL_REQUIRE(sign == 1.0f || sign == -1.0f, "half_padded: sign must be +-1");
+  BPL_REQUIRE(reinterpret_cast<uintptr_t>(dst) % 4 == 0, "half_padded: dst must be 4-byte aligned");
+  const int64_t total = rows * (Ls / 2);
+  const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 152 * 16));
+  half_padded_kernel<<<blocks, 256, 0, as_stream(stream)>>>(src, sign, static_cast<__half2*>(dst), rows, L, Ls);
+  BPL_CUDA_TRY(cudaGetLastError(), "half_padded launch");
+  return BPL_OK;
+}
 
 extern "C" int bpl_cost_from_sad(const float* sad, void* cost, int cost_half, int B, int H, int W, int D, int Ls,
                                  float temperature, void* stream) {

@@ -57,7 +57,7 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
                       float* grad_cost, float* grad_jump, float* grad_edge, void* workspace, size_t workspace_bytes,
                       int B, int H, int W, int L, int Lv, int jump_batch, int edge_batch, void* stream,
                       float* grad_messages = nullptr, int reps = 1, int64_t g_bstride = -1,
-                      int64_t g_sstride = -1) {
+                      int64_t g_sstride = -1, float cost_sign = 0.0f, int gc_ls = -1) {
   BPL_REQUIRE(variant >= 0 && variant <= 3, "lbp_backward: unknown variant %d", variant);
   // the pixel variant with the layer's two pairwise planes: same kernels, a
   // gradient of the planes' layout
@@ -74,6 +74,13 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   BPL_REQUIRE(argmin_kind >= BPL_ARGMIN_F32 && argmin_kind <= BPL_ARGMIN_U16, "lbp_backward: bad argmin kind");
   BPL_REQUIRE(edge_batch == 1 || edge_batch == B, "lbp_backward: edge batch %d must be 1 or B", edge_batch);
   const int Ls = (storage == 0) ? L : ((L + 7) & ~7);
+  // cost_sign 0: grad_cost is an output (zeroed here, label stride Ls);
+  // +-1: contributions are added, times cost_sign, onto what grad_cost holds
+  // (label stride gc_ls, L or Ls)
+  const bool accumulate = cost_sign != 0.0f;
+  if (gc_ls < 0) gc_ls = Ls;
+  BPL_REQUIRE(!accumulate || cost_sign == 1.0f || cost_sign == -1.0f, "lbp_backward: cost sign must be +-1");
+  BPL_REQUIRE(gc_ls == Ls || gc_ls == L, "lbp_backward: cost-gradient label stride %d must be L or Ls", gc_ls);
   BPL_REQUIRE(reps >= 1 && (reps == 1 || grad_messages == nullptr), "lbp_backward: bad pass count %d", reps);
   BPL_REQUIRE(workspace && workspace_bytes >= reps * bpl_lbp_backward_workspace_size(B, H, W, Ls),
               "lbp_backward: workspace of %zu bytes needed", reps * bpl_lbp_backward_workspace_size(B, H, W, Ls));
@@ -88,7 +95,8 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   if (variant == BPL_LBP_STEREO) gj_elems = static_cast<size_t>(jump_batch) * 4 * Lv * HW;
   else if (variant == BPL_LBP_SEM_GLOBAL) gj_elems = static_cast<size_t>(B) * 4 * L * L;
   else gj_elems = static_cast<size_t>(planes2 ? 2 : 4) * HW * L * L;
-  BPL_CUDA_TRY(cudaMemsetAsync(grad_cost, 0, sizeof(float) * B * HW * Ls, s), "lbp_backward: memset");
+  if (!accumulate)
+    BPL_CUDA_TRY(cudaMemsetAsync(grad_cost, 0, sizeof(float) * B * HW * Ls, s), "lbp_backward: memset");
   BPL_CUDA_TRY(cudaMemsetAsync(grad_jump, 0, sizeof(float) * gj_elems, s), "lbp_backward: memset");
   if (grad_edge)
     BPL_CUDA_TRY(cudaMemsetAsync(grad_edge, 0, sizeof(float) * edge_batch * 4 * HW, s), "lbp_backward: memset");
@@ -119,6 +127,8 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   a.jb = jump_batch;
   a.eb = edge_batch;
   a.argmin_kind = argmin_kind;
+  a.gc_ls = gc_ls;
+  a.gc_sign = accumulate ? cost_sign : 1.0f;
   a.planes2 = planes2;
   const int am_size = (argmin_kind == BPL_ARGMIN_U8) ? 1 : (argmin_kind == BPL_ARGMIN_U16 ? 2 : 4);
   if (storage == 0) {
@@ -199,6 +209,24 @@ extern "C" int bpl_lbp_backward_passes_f16(int variant, const float* jump, const
   return lbp_backward_impl(1, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
                            stream, nullptr, passes, in_grad_batch_stride, in_grad_slot_stride);
+}
+
+extern "C" int bpl_lbp_backward_passes_into(int storage, int variant, const float* jump, const float* edge,
+                                            const void* in_grad, int64_t in_grad_batch_stride,
+                                            int64_t in_grad_slot_stride, const void* messages, const void* argmin,
+                                            int argmin_kind, const float* scale, float* grad_cost, int grad_cost_ls,
+                                            float cost_sign, float* grad_jump, float* grad_edge, void* workspace,
+                                            size_t workspace_bytes, int B, int H, int W, int L, int Lv,
+                                            int jump_batch, int edge_batch, int passes, void* stream) {
+  BPL_TRACE("bpl_lbp_backward_passes_into");
+  BPL_REQUIRE(storage == 0 || storage == 1, "lbp_backward_passes_into: storage must be 0 or 1");
+  BPL_REQUIRE(cost_sign == 1.0f || cost_sign == -1.0f, "lbp_backward_passes_into: cost sign must be +-1");
+  BPL_REQUIRE(in_grad_batch_stride >= 0 && in_grad_slot_stride >= 0, "lbp_backward_passes: negative stride");
+  BPL_REQUIRE(in_grad != grad_cost, "lbp_backward_passes_into: in_grad must not alias grad_cost");
+  return lbp_backward_impl(storage, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
+                           grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
+                           stream, nullptr, passes, in_grad_batch_stride, in_grad_slot_stride, cost_sign,
+                           grad_cost_ls);
 }
 
 extern "C" int bpl_lbp_backward_f16(int variant, const float* jump, const float* edge, const void* in_grad,

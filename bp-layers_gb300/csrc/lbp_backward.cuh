@@ -76,6 +76,11 @@ struct BwdArgs {
   int64_t g_bstride, g_sstride;
   int Ls;
   int argmin_kind;
+  // grad_cost: label stride (Ls, or L for a gradient accumulated onto the
+  // layer's (B,H,W,L) cost gradient) and the sign its contributions are
+  // added with (+1; -1 when the buffer holds the gradient of -cost)
+  int gc_ls;
+  float gc_sign;
   int phase;  // 0: DOWN+UP over columns, 1: LEFT+RIGHT over rows
   int nchains;
   int ns;
@@ -215,7 +220,7 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
   const float* saved_up = a.saved + (static_cast<int64_t>(v) * 2 + 0) * HWL;
   const float* saved_dn = a.saved + (static_cast<int64_t>(v) * 2 + 1) * HWL;
   float* saved_out = a.saved + (static_cast<int64_t>(v) * 2 + (db == UP ? 0 : 1)) * HWL;
-  float* gcost_n = a.grad_cost + static_cast<int64_t>(n) * HWL;
+  float* gcost_n = a.grad_cost + static_cast<int64_t>(n) * HW * a.gc_ls;
   const float* edge_fd = a.edge + (static_cast<int64_t>(ne) * 4 + fd) * HW;
   const float* jump_fd = stereo ? a.jump + (static_cast<int64_t>(nj) * 4 + fd) * a.Lv * HW : nullptr;
   float* gjump_fd = stereo ? a.grad_jump + (static_cast<int64_t>(nj) * 4 + fd) * a.Lv * HW : nullptr;
@@ -503,14 +508,14 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
     // read back the chain accumulators (and clear the rows for the next
     // step); grad_cost[p][s] receives the row.  The rows are 32K
     // long, so labels >= L read zeros.
-    float* gc = gcost_n + static_cast<int64_t>(p) * Ls;
+    float* gc = gcost_n + static_cast<int64_t>(p) * a.gc_ls;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk) {
       const int t = lane + 32 * kk;
       accH[kk] = rowH[t];
       rowH[t] = 0.0f;
       const float v = accH[kk];
-      if (lvalid(kk) && v != 0.0f) atomicAdd(gc + t, v);
+      if (lvalid(kk) && v != 0.0f) atomicAdd(gc + t, a.gc_sign * v);
       if (!CROSS && lvalid(kk)) saved_out[static_cast<int64_t>(p) * Ls + t] = accH[kk];
       if (CROSS && a.gmsg != nullptr && lvalid(kk)) {
         float* gm = a.gmsg + static_cast<int64_t>(n) * 4 * HWL;

@@ -198,6 +198,25 @@ int bpl_lbp_backward_passes_f16(int variant, const float* jump, const float* edg
                                 int edge_batch, int passes, void* stream);
 
 /*
+ * bpl_lbp_backward_passes (storage 0, float messages) or
+ * bpl_lbp_backward_passes_f16 (storage 1) with the cost gradient added onto
+ * what grad_cost holds instead of written: each contribution times
+ * cost_sign (+1 or -1), label stride grad_cost_ls (L, or Lp = L rounded up
+ * to 8 for half storage).  grad_cost is not zeroed and must not alias
+ * in_grad.  The layer's fused backward passes the buffer holding the
+ * gradient of the probability volume (cost = -prob) from the belief
+ * epilogue, with cost_sign -1, so the sum and the negation of the two cost
+ * gradients cost no extra pass.  No counterpart in the reference (autograd
+ * adds the cost's gradients there).
+ */
+int bpl_lbp_backward_passes_into(int storage, int variant, const float* jump, const float* edge, const void* in_grad,
+                                 int64_t in_grad_batch_stride, int64_t in_grad_slot_stride, const void* messages,
+                                 const void* argmin, int argmin_kind, const float* scale, float* grad_cost,
+                                 int grad_cost_ls, float cost_sign, float* grad_jump, float* grad_edge,
+                                 void* workspace, size_t workspace_bytes, int B, int H, int W, int L, int Lv,
+                                 int jump_batch, int edge_batch, int passes, void* stream);
+
+/*
  * Exact adjoint of one LBP pass (FP32 storage).  No counterpart in the
  * reference, whose adjoint (bpl_lbp_backward) returns in_grad as the message
  * gradient; the cost, jump and edge gradients are the reference adjoint's
@@ -240,6 +259,29 @@ int bpl_beliefs_forward(const void* messages, int messages_half, const float* co
 int bpl_beliefs_backward(const void* messages, int messages_half, const float* cost, const float* temperature,
                          const float* beliefs, const float* grad_beliefs, float* grad_z, float* grad_temperature,
                          int B, int H, int W, int L, int Ls, void* stream);
+
+/*
+ * bpl_beliefs_forward with z = sum + cost_sign * cost (cost_sign +1 or -1:
+ * -1 reads the layer's probability volume, whose negation the cost is) and
+ * the cost in either storage: cost_half = 0, (B,H,W,L) float; 1, the
+ * FP16-storage volume (B,H,W,Ls) half (Ls = L rounded up to 8).
+ */
+int bpl_beliefs_forward_ex(const void* messages, int messages_half, const void* cost, int cost_half,
+                           float cost_sign, const float* temperature, float* beliefs, int B, int H, int W, int L,
+                           int Ls, void* stream);
+
+/*
+ * bpl_beliefs_backward for the layer's fused backward: cost and cost_sign as
+ * bpl_beliefs_forward_ex; grad_z (B,H,W,L) receives
+ * grad_z_sign (+1 or -1) times d loss / d z, and grad_copy, by copy_kind, a
+ * second copy of +d loss / d z: 0 none, 1 (B,H,W,Ls) half with the padding
+ * zeroed (the FP16 adjoint's in_grad), 2 (B,4,H,W,L) float in every message
+ * slot (the message gradient of a leaf message tensor), 3 (B,H,W,L) float.
+ */
+int bpl_beliefs_backward_ex(const void* messages, int messages_half, const void* cost, int cost_half,
+                            float cost_sign, const float* temperature, const float* beliefs, const float* grad_beliefs, float* grad_z,
+                            float grad_z_sign, void* grad_copy, int copy_kind, float* grad_temperature, int B, int H,
+                            int W, int L, int Ls, void* stream);
 
 /*
  * dst (B,4,n) = src (B,n) repeated over the four message slots; elements of
@@ -317,6 +359,14 @@ int bpl_pack_taps(const float* affinities, const float* offset, float* taps, int
  */
 int bpl_unpack_tap_grad(const float* grad_taps, float* grad_affinities, float* grad_offset, int N, int K, int H,
                         int W, void* stream);
+
+/*
+ * dst (rows, Ls) half = sign * src (rows, L) float (sign +1 or -1), labels
+ * L..Ls-1 zeroed, Ls = L rounded up to 8: the FP16-storage cost volume from
+ * the layer's probability volume (cost = -prob, ops/lbp_stereo/
+ * message_passing_op_cuda.py:162) in one pass.
+ */
+int bpl_half_padded(const float* src, float sign, void* dst, int64_t rows, int L, int Ls, void* stream);
 
 /* Disparity count D of the SAD volume: (int)((max_disp - min_disp + 1) / step)
  * (ops/sad/src/stereo_sad_kernel.cu:122); -1 for a non-positive step. */
