@@ -283,7 +283,9 @@ class BPLayerFn(torch.autograd.Function):
     sign -1, so autograd's sum of the cost's two gradients and the
     negation's backward take no pass and the adjoint no zero-fill; the
     beliefs' backward also writes the adjoint's in_grad (for a leaf message
-    tensor the materialised message gradient) in the same pass."""
+    tensor the materialised message gradient) in the same pass, and takes
+    z/T for the temperature's gradient from the beliefs and one float per
+    pixel the forward keeps, instead of re-reading messages and cost."""
 
     @staticmethod
     def forward(ctx, prob_vol, edge, messages, affinities, offset, T, iters, delta):
@@ -305,15 +307,16 @@ class BPLayerFn(torch.autograd.Function):
             else:
                 ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, messages, int(delta), argmin_dtype=am_dtype,
                                 argmin=argmins[k], scale=scales[k])
-        beliefs = ops.beliefs_forward_any_cost(messages, prob, T, L, cost_sign=-1.0)
-        ctx.save_for_backward(prob, taps, edge, messages, argmins, scales, T, beliefs)
+        lnorm = torch.empty((B, H, W), dtype=torch.float32, device=prob.device)
+        beliefs = ops.beliefs_forward_any_cost(messages, prob, T, L, cost_sign=-1.0, log_norm=lnorm)
+        ctx.save_for_backward(prob, taps, edge, messages, argmins, scales, T, beliefs, lnorm)
         ctx.half, ctx.L = half, L
         ctx.leaf_messages = messages.is_leaf
         return beliefs, messages
 
     @staticmethod
     def backward(ctx, grad_beliefs, grad_messages):
-        prob, taps, edge, messages, argmins, scales, T, beliefs = ctx.saved_tensors
+        prob, taps, edge, messages, argmins, scales, T, beliefs, lnorm = ctx.saved_tensors
         B, _, H, W, Ls = messages.shape
         need_m = ctx.needs_input_grad[2]
         if grad_beliefs is None:
@@ -325,7 +328,8 @@ class BPLayerFn(torch.autograd.Function):
         else:
             kind = ops.BELIEF_COPY_FLOAT
         gprob, gcopy, gT = ops.beliefs_backward_fused(messages, prob, T, beliefs, grad_beliefs, -1.0, kind,
-                                                      want_temperature=ctx.needs_input_grad[5], cost_sign=-1.0)
+                                                      want_temperature=ctx.needs_input_grad[5], cost_sign=-1.0,
+                                                      log_norm=lnorm)
         if grad_messages is not None:
             # the returned messages are used downstream too: their gradient
             # joins the beliefs' in every slot

@@ -580,10 +580,13 @@ def half_padded(src: torch.Tensor, sign: float = 1.0) -> torch.Tensor:
 
 
 def beliefs_forward_any_cost(messages: torch.Tensor, cost: torch.Tensor, temperature: torch.Tensor, L: int,
-                             out: torch.Tensor | None = None, cost_sign: float = 1.0) -> torch.Tensor:
+                             out: torch.Tensor | None = None, cost_sign: float = 1.0,
+                             log_norm: torch.Tensor | None = None) -> torch.Tensor:
     """beliefs_forward with z = sum + cost_sign * cost, the cost float
     (B,H,W,L) or the FP16-storage half volume (B,H,W,Lp)
-    (bpl_beliefs_forward_ex); cost_sign -1 takes the probability volume."""
+    (bpl_beliefs_forward_ex); cost_sign -1 takes the probability volume.
+    log_norm: a (B,H,W) float tensor receiving min(z/T) - log(sum) per
+    pixel, for beliefs_backward_fused."""
     _check_input("messages", messages, dtype=None, dim=5)
     _check_input("cost", cost, dtype=None, dim=4)
     B, _, H, W, Ls = messages.shape
@@ -591,7 +594,7 @@ def beliefs_forward_any_cost(messages: torch.Tensor, cost: torch.Tensor, tempera
         out = torch.empty((B, H, W, L), dtype=torch.float32, device=cost.device)
     st = _timed("beliefs_forward", lambda: lib().bpl_beliefs_forward_ex(
         _ptr(messages), int(messages.dtype == torch.float16), _ptr(cost), int(cost.dtype == torch.float16),
-        float(cost_sign), _ptr(temperature), _ptr(out), B, H, W, L, Ls, _stream(cost)))
+        float(cost_sign), _ptr(temperature), _ptr(out), _ptr(log_norm), B, H, W, L, Ls, _stream(cost)))
     check(st, "bpl_beliefs_forward_ex")
     return out
 
@@ -601,13 +604,16 @@ BELIEF_COPY_NONE, BELIEF_COPY_HALF, BELIEF_COPY_SLOTS, BELIEF_COPY_FLOAT = 0, 1,
 
 def beliefs_backward_fused(messages: torch.Tensor, cost: torch.Tensor, temperature: torch.Tensor,
                            beliefs: torch.Tensor, grad_beliefs: torch.Tensor, grad_z_sign: float, copy_kind: int,
-                           want_temperature: bool = True, cost_sign: float = 1.0):
+                           want_temperature: bool = True, cost_sign: float = 1.0,
+                           log_norm: torch.Tensor | None = None):
     """Gradient of the fused epilogue for the layer's fused backward
     (bpl_beliefs_backward_ex): returns (grad_z_sign * grad_z (B,H,W,L),
     the copy of +grad_z selected by copy_kind or None, grad_T or None).
     copy_kind: BELIEF_COPY_HALF (B,1,H,W,Lp) half, BELIEF_COPY_SLOTS
     (B,4,H,W,L) float, BELIEF_COPY_FLOAT (B,1,H,W,L) float; cost and
-    cost_sign as beliefs_forward_any_cost."""
+    cost_sign as beliefs_forward_any_cost.  With the forward's log_norm the
+    temperature's gradient takes z/T from the beliefs (messages and cost are
+    not read)."""
     _check_input("beliefs", beliefs, dim=4)
     grad_beliefs = grad_beliefs.contiguous()
     _check_input("grad_beliefs", grad_beliefs, dim=4)
@@ -627,8 +633,7 @@ def beliefs_backward_fused(messages: torch.Tensor, cost: torch.Tensor, temperatu
     st = _timed("beliefs_backward", lambda: lib().bpl_beliefs_backward_ex(
         _ptr(messages), int(messages.dtype == torch.float16), _ptr(cost), int(cost.dtype == torch.float16),
         float(cost_sign), _ptr(temperature), _ptr(beliefs), _ptr(grad_beliefs), _ptr(gz), float(grad_z_sign),
-        _ptr(copy), copy_kind,
-        _ptr(gT), B, H, W, L, Ls, _stream(beliefs)))
+        _ptr(copy), copy_kind, _ptr(gT), _ptr(log_norm), B, H, W, L, Ls, _stream(beliefs)))
     check(st, "bpl_beliefs_backward_ex")
     return gz, copy, gT
 

@@ -57,9 +57,13 @@ __device__ __forceinline__ void load_z(const T* msgs, const TC* cost, float csig
   }
 }
 
+// lnorm (B,H,W), may be null: per pixel c = min(z/T) - log(sum), with which
+// the backward recovers z/T = c - log(beliefs) without re-reading messages
+// and cost.
 template <int K, typename T, typename TC>
 __global__ void __launch_bounds__(256) beliefs_fwd_kernel(const T* msgs, const TC* cost, float csign, const float* Tp,
-                                                          float* out, int B, int H, int W, int L, int Ls) {
+                                                          float* out, float* lnorm, int B, int H, int W, int L,
+                                                          int Ls) {
   const int lane = threadIdx.x & 31;
   const int64_t HW = static_cast<int64_t>(H) * W;
   const int64_t npix = B * HW;
@@ -84,6 +88,7 @@ __global__ void __launch_bounds__(256) beliefs_fwd_kernel(const T* msgs, const T
     }
     s = warp_sum(s);
     const float inv = 1.0f / s;
+    if (lnorm != nullptr && lane == 0) lnorm[pix] = mn - logf(s);
     float* o = out + pix * L;
 #pragma unroll
     for (int k = 0; k < K; ++k)
@@ -94,14 +99,18 @@ __global__ void __launch_bounds__(256) beliefs_fwd_kernel(const T* msgs, const T
 // Gradient outputs: gz (B,H,W,L) float receives gz_sign * dL/dz; `copy`, by
 // copy_kind, a second copy of +dL/dz: kCopyHalf (B,H,W,Ls) half with the
 // padding zeroed, kCopySlots (B,4,H,W,L) float in every message slot,
-// kCopyFloat (B,H,W,L) float.
+// kCopyFloat (B,H,W,L) float.  The temperature's gradient needs z / T:
+// from lnorm (the forward's c) as c - log(beliefs) when given (a label whose
+// belief is 0 has du = 0 and adds nothing; labels of tiny beliefs, where the
+// log is coarse, add du * z / T with du of their size), else recomputed from
+// messages and cost.
 enum { kCopyNone = 0, kCopyHalf = 1, kCopySlots = 2, kCopyFloat = 3 };
 
 template <int K, typename T, typename TC>
 __global__ void __launch_bounds__(256) beliefs_bwd_kernel(const T* msgs, const TC* cost, float csign, const float* Tp,
                                                           const float* y, const float* gy, float* gz, float gz_sign,
-                                                          void* copy, int copy_kind, float* gT, int B, int H, int W,
-                                                          int L, int Ls) {
+                                                          void* copy, int copy_kind, float* gT, const float* lnorm,
+                                                          int B, int H, int W, int L, int Ls) {
   const int lane = threadIdx.x & 31;
   const int64_t HW = static_cast<int64_t>(H) * W;
   const int64_t npix = B * HW;
@@ -113,7 +122,7 @@ __global__ void __launch_bounds__(256) beliefs_bwd_kernel(const T* msgs, const T
        pix += warps) {
     const int n = static_cast<int>(pix / HW);
     float zt[K];
-    if (gT != nullptr) load_z<K, T, TC>(msgs, cost, csign, pix, HWLs, Ls, L, n, HW, Tm, lane, zt);
+    if (gT != nullptr && lnorm == nullptr) load_z<K, T, TC>(msgs, cost, csign, pix, HWLs, Ls, L, n, HW, Tm, lane, zt);
     const float* yp = y + pix * L;
     const float* gp = gy + pix * L;
     float yv[K], gv[K], d = 0.0f;
@@ -125,6 +134,11 @@ __global__ void __launch_bounds__(256) beliefs_bwd_kernel(const T* msgs, const T
       d += yv[k] * gv[k];
     }
     d = warp_sum(d);
+    if (gT != nullptr && lnorm != nullptr) {
+      const float c = __ldg(lnorm + pix);
+#pragma unroll
+      for (int k = 0; k < K; ++k) zt[k] = (yv[k] > 0.0f) ? c - logf(yv[k]) : 0.0f;
+    }
     float* o = gz + pix * L;
     const int64_t p = pix % HW;
 #pragma unroll
@@ -161,10 +175,11 @@ int grid_for(int64_t npix) {
 
 template <typename T, typename TC>
 int fwd_impl(const T* msgs, const TC* cost, const float* Tm, float* out, int B, int H, int W, int L, int Ls,
-             cudaStream_t s, float csign = 1.0f) {
+             cudaStream_t s, float csign = 1.0f, float* lnorm = nullptr) {
   const int g = grid_for(static_cast<int64_t>(B) * H * W);
   const int k = (L + 31) / 32;
-#define BPL_BFWD(KK) beliefs_fwd_kernel<KK, T, TC><<<g, 256, 0, s>>>(msgs, cost, csign, Tm, out, B, H, W, L, Ls)
+#define BPL_BFWD(KK) \
+  beliefs_fwd_kernel<KK, T, TC><<<g, 256, 0, s>>>(msgs, cost, csign, Tm, out, lnorm, B, H, W, L, Ls)
   if (k <= 1) BPL_BFWD(1);
   else if (k <= 2) BPL_BFWD(2);
   else if (k <= 4) BPL_BFWD(4);
@@ -180,13 +195,13 @@ int fwd_impl(const T* msgs, const TC* cost, const float* Tm, float* out, int B, 
 template <typename T, typename TC>
 int bwd_impl(const T* msgs, const TC* cost, const float* Tm, const float* y, const float* gy, float* gz, float* gT,
              int B, int H, int W, int L, int Ls, cudaStream_t s, float gz_sign = 1.0f, void* copy = nullptr,
-             int copy_kind = kCopyNone, float csign = 1.0f) {
+             int copy_kind = kCopyNone, float csign = 1.0f, const float* lnorm = nullptr) {
   if (gT) BPL_CUDA_TRY(cudaMemsetAsync(gT, 0, sizeof(float), s), "beliefs_backward: memset");
   const int g = grid_for(static_cast<int64_t>(B) * H * W);
   const int k = (L + 31) / 32;
 #define BPL_BBWD(KK)                                                                                  \
-  beliefs_bwd_kernel<KK, T, TC><<<g, 256, 0, s>>>(msgs, cost, csign, Tm, y, gy, gz, gz_sign, copy, copy_kind, gT, B, \
-                                                  H, W, L, Ls)
+  beliefs_bwd_kernel<KK, T, TC><<<g, 256, 0, s>>>(msgs, cost, csign, Tm, y, gy, gz, gz_sign, copy, copy_kind, gT, \
+                                                  lnorm, B, H, W, L, Ls)
   if (k <= 1) BPL_BBWD(1);
   else if (k <= 2) BPL_BBWD(2);
   else if (k <= 4) BPL_BBWD(4);
@@ -261,8 +276,8 @@ extern "C" int bpl_beliefs_forward(const void* messages, int messages_half, cons
 }
 
 extern "C" int bpl_beliefs_forward_ex(const void* messages, int messages_half, const void* cost, int cost_half,
-                                      float cost_sign, const float* temperature, float* beliefs, int B, int H, int W,
-                                      int L, int Ls, void* stream) {
+                                      float cost_sign, const float* temperature, float* beliefs, float* log_norm,
+                                      int B, int H, int W, int L, int Ls, void* stream) {
   BPL_TRACE("bpl_beliefs_forward_ex");
   BPL_REQUIRE(messages && cost && beliefs && temperature, "beliefs_forward: null pointer");
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1 && L >= 1 && L <= 1024 && Ls >= L, "beliefs_forward: bad shape");
@@ -270,23 +285,25 @@ extern "C" int bpl_beliefs_forward_ex(const void* messages, int messages_half, c
   BPL_REQUIRE(cost_sign == 1.0f || cost_sign == -1.0f, "beliefs_forward: cost sign must be +-1");
   cudaStream_t st = as_stream(stream);
   const float cs = cost_sign;
+  float* ln = log_norm;
   if (messages_half) {
     const __half* m = static_cast<const __half*>(messages);
-    return cost_half ? fwd_impl(m, static_cast<const __half*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs)
-                     : fwd_impl(m, static_cast<const float*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs);
+    return cost_half ? fwd_impl(m, static_cast<const __half*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs, ln)
+                     : fwd_impl(m, static_cast<const float*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs, ln);
   }
   const float* m = static_cast<const float*>(messages);
-  return cost_half ? fwd_impl(m, static_cast<const __half*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs)
-                   : fwd_impl(m, static_cast<const float*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs);
+  return cost_half ? fwd_impl(m, static_cast<const __half*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs, ln)
+                   : fwd_impl(m, static_cast<const float*>(cost), temperature, beliefs, B, H, W, L, Ls, st, cs, ln);
 }
 
 extern "C" int bpl_beliefs_backward_ex(const void* messages, int messages_half, const void* cost, int cost_half,
                                        float cost_sign, const float* temperature, const float* beliefs, const float* grad_beliefs,
                                        float* grad_z, float grad_z_sign, void* grad_copy, int copy_kind,
-                                       float* grad_temperature, int B, int H, int W, int L, int Ls, void* stream) {
+                                       float* grad_temperature, const float* log_norm, int B, int H, int W, int L,
+                                       int Ls, void* stream) {
   BPL_TRACE("bpl_beliefs_backward_ex");
   BPL_REQUIRE(beliefs && grad_beliefs && grad_z && temperature, "beliefs_backward: null pointer");
-  BPL_REQUIRE(grad_temperature == nullptr || (messages && cost), "beliefs_backward: null messages/cost");
+  BPL_REQUIRE(grad_temperature == nullptr || log_norm || (messages && cost), "beliefs_backward: null messages/cost");
   BPL_REQUIRE(B >= 1 && H >= 1 && W >= 1 && L >= 1 && L <= 1024 && Ls >= L, "beliefs_backward: bad shape");
   BPL_REQUIRE(!cost_half || Ls == ((L + 7) & ~7), "beliefs_backward: a half cost has the padded label stride");
   BPL_REQUIRE(grad_z_sign == 1.0f || grad_z_sign == -1.0f, "beliefs_backward: sign must be +-1");
@@ -297,7 +314,7 @@ extern "C" int bpl_beliefs_backward_ex(const void* messages, int messages_half, 
   cudaStream_t st = as_stream(stream);
 #define BPL_BBWD_EX(MT, CT)                                                                                      \
   bwd_impl(static_cast<const MT*>(messages), static_cast<const CT*>(cost), temperature, beliefs, grad_beliefs, \
-           grad_z, grad_temperature, B, H, W, L, Ls, st, grad_z_sign, grad_copy, copy_kind, cost_sign)
+           grad_z, grad_temperature, B, H, W, L, Ls, st, grad_z_sign, grad_copy, copy_kind, cost_sign, log_norm)
   if (messages_half) return cost_half ? BPL_BBWD_EX(__half, __half) : BPL_BBWD_EX(__half, float);
   return cost_half ? BPL_BBWD_EX(float, __half) : BPL_BBWD_EX(float, float);
 #undef BPL_BBWD_EX

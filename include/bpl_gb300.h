@@ -264,11 +264,14 @@ int bpl_beliefs_backward(const void* messages, int messages_half, const float* c
  * bpl_beliefs_forward with z = sum + cost_sign * cost (cost_sign +1 or -1:
  * -1 reads the layer's probability volume, whose negation the cost is) and
  * the cost in either storage: cost_half = 0, (B,H,W,L) float; 1, the
- * FP16-storage volume (B,H,W,Ls) half (Ls = L rounded up to 8).
+ * FP16-storage volume (B,H,W,Ls) half (Ls = L rounded up to 8).  log_norm
+ * (B,H,W) float, may be NULL: per pixel c = min(z/T) - log(sum of the
+ * softmin's exps), from which bpl_beliefs_backward_ex recovers z/T as
+ * c - log(beliefs).
  */
 int bpl_beliefs_forward_ex(const void* messages, int messages_half, const void* cost, int cost_half,
-                           float cost_sign, const float* temperature, float* beliefs, int B, int H, int W, int L,
-                           int Ls, void* stream);
+                           float cost_sign, const float* temperature, float* beliefs, float* log_norm, int B, int H,
+                           int W, int L, int Ls, void* stream);
 
 /*
  * bpl_beliefs_backward for the layer's fused backward: cost and cost_sign as
@@ -277,11 +280,14 @@ int bpl_beliefs_forward_ex(const void* messages, int messages_half, const void* 
  * second copy of +d loss / d z: 0 none, 1 (B,H,W,Ls) half with the padding
  * zeroed (the FP16 adjoint's in_grad), 2 (B,4,H,W,L) float in every message
  * slot (the message gradient of a leaf message tensor), 3 (B,H,W,L) float.
+ * log_norm: the forward's, or NULL to recompute z from messages and cost for
+ * grad_temperature (with it, messages and cost are not read and may be
+ * NULL).
  */
 int bpl_beliefs_backward_ex(const void* messages, int messages_half, const void* cost, int cost_half,
                             float cost_sign, const float* temperature, const float* beliefs, const float* grad_beliefs, float* grad_z,
-                            float grad_z_sign, void* grad_copy, int copy_kind, float* grad_temperature, int B, int H,
-                            int W, int L, int Ls, void* stream);
+                            float grad_z_sign, void* grad_copy, int copy_kind, float* grad_temperature,
+                            const float* log_norm, int B, int H, int W, int L, int Ls, void* stream);
 
 /*
  * dst (B,4,n) = src (B,n) repeated over the four message slots; elements of
