@@ -111,7 +111,6 @@ BPL_HD float mul_(float a, float b) { return __fmul_rn(a, b); }
 BPL_HD float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 BPL_HD int f2i(float f) { return __float_as_int(f); }
 BPL_HD float i2f(int i) { return __int_as_float(i); }
-BPL_HD float rint_(float f) { return rintf(f); }
 #else
 inline float add_(float a, float b) { volatile float r = a + b; return r; }
 inline float sub_(float a, float b) { volatile float r = a - b; return r; }
@@ -119,7 +118,6 @@ inline float mul_(float a, float b) { volatile float r = a * b; return r; }
 inline float fma_(float a, float b, float c) { return std::fmaf(a, b, c); }
 inline int f2i(float f) { int i; std::memcpy(&i, &f, 4); return i; }
 inline float i2f(int i) { float f; std::memcpy(&f, &i, 4); return f; }
-inline float rint_(float f) { return std::nearbyint(f); }
 #endif
 
 BPL_HD void two_sum(float a, float b, float& s, float& e) {
@@ -147,8 +145,13 @@ BPL_HD float half_ulp_side(float z, float d) {
 // when the caller must evaluate the reference expression instead.
 BPL_HD bool exp_fast(float x, float& out, const float* exp_hi = kTab.exp_hi, const float* exp_lo = kTab.exp_lo) {
   if (!(x > -87.0f && x < 88.0f)) return false;
-  const float N = rint_(mul_(x, 92.332482616893656f));  // 64/ln2
-  const int n = static_cast<int>(N);
+  // N = rint(x * 64/ln2) by the 1.5 * 2^23 shift: |x * 64/ln2| < 2^13, so the
+  // sum lies in [2^23, 2^24), where the float spacing is 1 and the addition
+  // rounds to the nearest integer (ties to even, as rint); n is read from
+  // the sum's bits (no float-to-int conversion on the chain)
+  const float tN = add_(mul_(x, 92.332482616893656f), 12582912.0f);  // 64/ln2, 1.5 * 2^23
+  const float N = sub_(tN, 12582912.0f);                              // exact
+  const int n = f2i(tN) - 0x4b400000;
   const int j = n & 63;
   const int m = n >> 6;
   // r = x - N * ln2/64 as a float-float (rh, rl)
@@ -191,8 +194,11 @@ BPL_HD bool log_fast(float s, float& out) {
   if (!(s > 0.0f) || (bits & 0x7f800000) == 0 || (bits & 0x7f800000) == 0x7f800000) return false;
   const int e = ((bits >> 23) & 0xff) - 127;
   const float mnt = i2f((bits & 0x007fffff) | 0x3f800000);
-  const int j = static_cast<int>(add_(mul_(sub_(mnt, 1.0f), 64.0f), 0.5f));
-  const float F = add_(1.0f, mul_(static_cast<float>(j), 0.015625f));
+  // j = (int)(64 (mnt - 1) + 0.5) and F = 1 + j/64, both exact, from the
+  // mantissa bits m: 64 (mnt - 1) = m 2^-17, so j = (m + 2^16) >> 17 and F
+  // has mantissa field j << 17 (j = 64 gives 2.0)
+  const int j = ((bits & 0x007fffff) + (1 << 16)) >> 17;
+  const float F = i2f(0x3f800000 + (j << 17));
   const float f = sub_(mnt, F);  // exact
   const float inv = kTab.inv[j];
   const float uh = mul_(f, inv);

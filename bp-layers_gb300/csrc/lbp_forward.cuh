@@ -768,6 +768,11 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
       int R = -2;
       int s1 = -1;
       int wcode = kWinGeneric;
+      // The tie-only count's two reductions are issued here and first read
+      // after the window terms below, which run in their shadow: the count
+      // only sends the step to the full scan (several senders) or names the
+      // one sender s1 for the fix.
+      int nn = 0, smax = -1;
       if (NW == 1 && stereo) {
         wcode = __float_as_int(tile[(a.Lv + 2) * 33 + j]);
         if ((wcode & 0xff) != kWinGeneric) {
@@ -781,20 +786,19 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
               lc += nr ? 1 : 0;
               ll = nr ? c.t0 + lane + 32 * kk : ll;
             }
-            const int nn = __reduce_add_sync(FULL, lc);
-            if (nn > 1) R = -2;
-            else if (nn == 1) s1 = __reduce_max_sync(FULL, ll);
+            nn = __reduce_add_sync(FULL, lc);
+            smax = __reduce_max_sync(FULL, ll);
           }
         }
       }
       bool own[KW];
+      float mw[KW];
+      int aw[KW];
+      const int c0 = a.Lv / 2;
       if (R >= -1) {
         // the 2R+1 beating terms of every label, straight-line per path
         // (uniform branches outside the label loops keep the slots
         // independent); hs holds +inf outside [0, L)
-        float mw[KW];
-        int aw[KW];
-        const int c0 = a.Lv / 2;
         if (R == 1) {
           const float fm1 = tile[min(a.Lv - 1, c0 + 1) * 33 + j];  // sender t-1
           const float f00 = tile[c0 * 33 + j];                     // sender t
@@ -841,6 +845,10 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
             aw[kk] = 0;
           }
         }
+      }
+      if (nn > 1) R = -2;
+      else if (nn == 1) s1 = smax;
+      if (R >= -1) {
 #pragma unroll
         for (int kk = 0; kk < KW; ++kk) {
           const bool valid = lvalid(kk);
