@@ -372,8 +372,9 @@ def run_ours(args):
                       "forward_GBps_21B": U_pass * FWD_BYTES_PER_UPDATE / (fwd_ms / 1e3) / 1e9 if fwd else None,
                       "backward_GBps_17B": U_pass * BWD_BYTES_PER_UPDATE / (bwd_ms / 1e3) / 1e9 if bwd else None},
         # forward passes (2 phases each), batched adjoint (2 phases), belief
-        # epilogue (forward, backward), the initial messages' gradient
-        "gpu_launches": args.steps * (ITERS * 2 + 2 + 2 + 1),
+        # epilogue (forward; backward, which also writes the initial
+        # messages' gradient), tap packing and its gradient's fold
+        "gpu_launches": args.steps * (ITERS * 2 + 2 + 2 + 2),
         "fp16": fp16,
         "recompute_argmin": recompute,
         "clocks": clk.summary(),
