@@ -32,7 +32,7 @@ SIGNATURES = {
     "bpl_lbp_backward_passes_f16": [c_int] + [c_void_p] * 3 + [ctypes.c_int64] * 2 + [c_void_p] * 2 + [c_int] + [c_void_p] * 5 + [ctypes.c_size_t] + [c_int] * 8 + [c_void_p],
     "bpl_beliefs_forward": [c_void_p, c_int] + [c_void_p] * 3 + [c_int] * 5 + [c_void_p],
     "bpl_beliefs_backward": [c_void_p, c_int] + [c_void_p] * 6 + [c_int] * 5 + [c_void_p],
-    "bpl_lbp_backward_passes_into": [c_int, c_int] + [c_void_p] * 3 + [ctypes.c_int64] * 2 + [c_void_p] * 2 + [c_int] + [c_void_p] * 2 + [c_int, c_float] + [c_void_p] * 3 + [ctypes.c_size_t] + [c_int] * 8 + [c_void_p],
+    "bpl_lbp_backward_passes_into": [c_int, c_int] + [c_void_p] * 3 + [ctypes.c_int64] * 2 + [c_void_p] * 2 + [c_int] + [c_void_p] * 2 + [c_int, c_float] + [c_void_p] * 3 + [ctypes.c_size_t] + [c_int] * 9 + [c_void_p],
     "bpl_beliefs_forward_ex": [c_void_p, c_int, c_void_p, c_int, c_float] + [c_void_p] * 3 + [c_int] * 5 + [c_void_p],
     "bpl_beliefs_backward_ex": [c_void_p, c_int, c_void_p, c_int, c_float] + [c_void_p] * 4 + [c_float, c_void_p, c_int, c_void_p, c_void_p] + [c_int] * 5 + [c_void_p],
     "bpl_half_padded": [c_void_p, c_float, c_void_p, ctypes.c_int64, c_int, c_int, c_void_p],

@@ -338,8 +338,11 @@ class BPLayerFn(torch.autograd.Function):
             gin = gcopy
         else:
             gin = gcopy.expand(B, 4, H, W, gcopy.shape[-1])
+        # the packed taps of 3 affinities ([offset, L2, L1, 0, L1, L2]): the
+        # adjoint bins for the fold below (taps 1 and 5 summed, tap 3 dropped)
         _, gtaps, ge = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, gin, messages, argmins, scales, L=ctx.L,
-                                               grad_cost_into=gprob, cost_sign=-1.0)
+                                               grad_cost_into=gprob, cost_sign=-1.0,
+                                               layer_taps=taps.shape[2] == 6)
         g_aff, g_off = unpack_affinity_grad(gtaps)
         gm = None
         if need_m:

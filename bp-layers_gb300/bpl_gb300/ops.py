@@ -422,7 +422,7 @@ def lbp_backward_f16(variant: int, jump, edge: torch.Tensor, in_grad_h: torch.Te
 def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.Tensor, messages: torch.Tensor,
                         argmins: torch.Tensor, scales: torch.Tensor, L: int | None = None,
                         workspace: torch.Tensor | None = None, grad_cost_into: torch.Tensor | None = None,
-                        cost_sign: float = 1.0):
+                        cost_sign: float = 1.0, layer_taps: bool = False):
     """Reference adjoint of P passes run in place on one messages tensor,
     in one launch: argmins (P,B,4,H,W,Ls) and scales (P,B,4,H,W) stacked in
     pass order; in_grad and messages shared (the reference's backward of each
@@ -434,7 +434,11 @@ def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.T
 
     grad_cost_into: a float (B,H,W,L) or (B,H,W,Ls) tensor the cost
     gradient is added onto, times cost_sign (+1 or -1), instead of a new
-    zeroed one (bpl_lbp_backward_passes_into); it is returned as grad_cost."""
+    zeroed one (bpl_lbp_backward_passes_into); it is returned as grad_cost.
+    layer_taps (with grad_cost_into; stereo, 6 taps): jump is the layer's
+    packed taps [offset, L2, L1, 0, L1, L2] and grad_jump holds what the
+    layer's fold needs (the L2 taps' gradient summed in tap 1, taps 3 and 5
+    none)."""
     half = messages.dtype == torch.float16
     if not isinstance(in_grad, torch.Tensor) or in_grad.dtype != messages.dtype or in_grad.dim() != 5 \
             or not in_grad.is_cuda:
@@ -484,6 +488,8 @@ def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.T
     name = "lbp_backward_f16" if half else "lbp_backward"
     ws_bytes = workspace.numel() * workspace.element_size()
     jp = _ptr(jump) if not _pixel(variant) else None
+    if layer_taps and (grad_cost_into is None or variant != LBP_STEREO or Lv != 6):
+        raise BplError("layer_taps: stereo with 6 taps, through grad_cost_into")
     if grad_cost_into is None:
         grad_cost = torch.empty((B, H, W, Ls), dtype=torch.float32, device=dev)
         fn = lib().bpl_lbp_backward_passes_f16 if half else lib().bpl_lbp_backward_passes
@@ -501,7 +507,8 @@ def lbp_backward_passes(variant: int, jump, edge: torch.Tensor, in_grad: torch.T
         st = _timed(name, lambda: lib().bpl_lbp_backward_passes_into(
             int(half), variant, jp, _ptr(edge), _ptr(in_grad), g_bstride, g_sstride, _ptr(messages), _ptr(argmins),
             kind, _ptr(scales), _ptr(grad_cost), grad_cost.shape[3], float(cost_sign), _ptr(grad_jump),
-            _ptr(grad_edge), _ptr(workspace), ws_bytes, B, H, W, L, Lv, jb, edge.shape[0], P, _stream(messages)))
+            _ptr(grad_edge), _ptr(workspace), ws_bytes, B, H, W, L, Lv, jb, edge.shape[0], P, int(bool(layer_taps)),
+            _stream(messages)))
     check(st, "bpl_lbp_backward_passes")
     return grad_cost, grad_jump, grad_edge
 

@@ -155,6 +155,24 @@ __device__ __forceinline__ float warp_reduce_scatter8(const float (&v)[8], int l
   return w1;
 }
 
+// The same for four values: value q summed over the warp ends in lanes
+// 8q .. 8q+7.
+__device__ __forceinline__ float warp_reduce_scatter4(const float (&v)[4], int lane) {
+  const bool h16 = lane & 16, h8 = lane & 8;
+  float w2[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const float keep = h16 ? v[i + 2] : v[i];
+    const float send = h16 ? v[i] : v[i + 2];
+    w2[i] = keep + __shfl_xor_sync(FULL, send, 16);
+  }
+  float w1 = (h8 ? w2[1] : w2[0]) + __shfl_xor_sync(FULL, h8 ? w2[0] : w2[1], 8);
+  w1 += __shfl_xor_sync(FULL, w1, 4);
+  w1 += __shfl_xor_sync(FULL, w1, 2);
+  w1 += __shfl_xor_sync(FULL, w1, 1);
+  return w1;
+}
+
 // Plain warp sum (any order) for the adjoint kernels, which have no bitwise
 // parity target (the reference uses float atomics).
 __device__ __forceinline__ float warp_sum(float v) {

@@ -57,7 +57,7 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
                       float* grad_cost, float* grad_jump, float* grad_edge, void* workspace, size_t workspace_bytes,
                       int B, int H, int W, int L, int Lv, int jump_batch, int edge_batch, void* stream,
                       float* grad_messages = nullptr, int reps = 1, int64_t g_bstride = -1,
-                      int64_t g_sstride = -1, float cost_sign = 0.0f, int gc_ls = -1) {
+                      int64_t g_sstride = -1, float cost_sign = 0.0f, int gc_ls = -1, int layer_taps = 0) {
   BPL_REQUIRE(variant >= 0 && variant <= 3, "lbp_backward: unknown variant %d", variant);
   // the pixel variant with the layer's two pairwise planes: same kernels, a
   // gradient of the planes' layout
@@ -84,6 +84,8 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   BPL_REQUIRE(reps >= 1 && (reps == 1 || grad_messages == nullptr), "lbp_backward: bad pass count %d", reps);
   BPL_REQUIRE(workspace && workspace_bytes >= reps * bpl_lbp_backward_workspace_size(B, H, W, Ls),
               "lbp_backward: workspace of %zu bytes needed", reps * bpl_lbp_backward_workspace_size(B, H, W, Ls));
+  BPL_REQUIRE(!layer_taps || (variant == BPL_LBP_STEREO && Lv == 6),
+              "lbp_backward: the layer's packed taps are stereo taps with Lv = 6");
   if (variant == BPL_LBP_STEREO) {
     BPL_REQUIRE(Lv >= 2 && Lv <= 16, "lbp_backward: Lv=%d outside [2, 16]", Lv);
     BPL_REQUIRE(jump_batch == 1 || jump_batch == B, "lbp_backward: jump batch %d must be 1 or B", jump_batch);
@@ -130,6 +132,7 @@ int lbp_backward_impl(int storage, int variant, const float* jump, const float* 
   a.gc_ls = gc_ls;
   a.gc_sign = accumulate ? cost_sign : 1.0f;
   a.planes2 = planes2;
+  a.layer_taps = layer_taps ? 1 : 0;
   const int am_size = (argmin_kind == BPL_ARGMIN_U8) ? 1 : (argmin_kind == BPL_ARGMIN_U16 ? 2 : 4);
   if (storage == 0) {
     a.lrow = bwd::a4(L);
@@ -217,7 +220,8 @@ extern "C" int bpl_lbp_backward_passes_into(int storage, int variant, const floa
                                             int argmin_kind, const float* scale, float* grad_cost, int grad_cost_ls,
                                             float cost_sign, float* grad_jump, float* grad_edge, void* workspace,
                                             size_t workspace_bytes, int B, int H, int W, int L, int Lv,
-                                            int jump_batch, int edge_batch, int passes, void* stream) {
+                                            int jump_batch, int edge_batch, int passes, int layer_taps,
+                                            void* stream) {
   BPL_TRACE("bpl_lbp_backward_passes_into");
   BPL_REQUIRE(storage == 0 || storage == 1, "lbp_backward_passes_into: storage must be 0 or 1");
   BPL_REQUIRE(cost_sign == 1.0f || cost_sign == -1.0f, "lbp_backward_passes_into: cost sign must be +-1");
@@ -226,7 +230,7 @@ extern "C" int bpl_lbp_backward_passes_into(int storage, int variant, const floa
   return lbp_backward_impl(storage, variant, jump, edge, in_grad, messages, argmin, argmin_kind, scale, grad_cost,
                            grad_jump, grad_edge, workspace, workspace_bytes, B, H, W, L, Lv, jump_batch, edge_batch,
                            stream, nullptr, passes, in_grad_batch_stride, in_grad_slot_stride, cost_sign,
-                           grad_cost_ls);
+                           grad_cost_ls, layer_taps);
 }
 
 extern "C" int bpl_lbp_backward_f16(int variant, const float* jump, const float* edge, const void* in_grad,

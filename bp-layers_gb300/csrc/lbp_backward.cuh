@@ -81,6 +81,12 @@ struct BwdArgs {
   // added with (+1; -1 when the buffer holds the gradient of -cost)
   int gc_ls;
   float gc_sign;
+  // jump holds the stereo layer's packed taps [offset, L2, L1, 0, L1, L2]
+  // (Lv = 6): taps 1 and 5 carry the same value and the layer's fold adds
+  // their gradients, tap 3 is 0 and its gradient is dropped.  The adjoint
+  // then bins three ways (|d| >= 2, d = -1, d = +1) and writes the L2
+  // gradient to tap 1 only, nothing to taps 3 and 5.
+  int layer_taps;
   int phase;  // 0: DOWN+UP over columns, 1: LEFT+RIGHT over rows
   int nchains;
   int ns;
@@ -162,9 +168,10 @@ constexpr int bwd_warps_per_block() { return (CROSS || K > 8) ? 4 : 2; }
 template <bool CROSS, int K>
 constexpr int bwd_min_blocks() { return K > 8 ? 1 : (CROSS ? 4 : 9); }
 
-template <int K, int VARIANT, int LV, bool CROSS, typename T>
+template <int K, int VARIANT, int LV, bool CROSS, typename T, bool LT = false>
 __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_blocks<CROSS, K>())
     lbp_backward_kernel(BwdArgs a) {
+  static_assert(!LT || (VARIANT == BPL_LBP_STEREO && LV == 6), "layer taps: stereo, 6 taps");
   using namespace bwd;
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
@@ -386,10 +393,13 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
     // global minimum of h, for every label farther than the truncation window
     // from it): that group is summed with warp shuffles, the few others go
     // through shared-memory atomics with little contention.
+    // the slot of label L-1: K-1 where K = ceil(L/32) (the stereo and global
+    // dispatch), else from L
+    const int kL = (VARIANT != BPL_LBP_SEM_PIXEL && K <= 8) ? K - 1 : ((L - 1) >> 5);
     int amL = 0;
 #pragma unroll
     for (int kk = 0; kk < K; ++kk)
-      if (kk == ((L - 1) >> 5)) amL = am[kk];
+      if (kk == kL) amL = am[kk];
     const int g0 = __shfl_sync(FULL, am[0], 0);
     const int gL = __shfl_sync(FULL, amL, (L - 1) & 31);
     // the dominant group: the first and last labels' shared argmin (labels
@@ -429,7 +439,30 @@ __global__ void __launch_bounds__(32 * bwd_warps_per_block<CROSS, K>(), bwd_min_
     // tap index clamp(Lv/2 + t - s*), reduced together with the dominant
     // group's sums (tap bins in values 3..7 for Lv <= 6, else a second pass)
     float ge = 0.0f;
-    if (stereo) {
+    if (LT) {
+      // the layer's taps: bins |d| >= 2 (taps 1 and 5), d = -1 (tap 2),
+      // d = +1 (tap 4), d = t - s*; reduced with the dominant sum (values
+      // 0..3 at lanes 0, 8, 16, 24)
+      float v4[4] = {dsum[0], 0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int kk = 0; kk < K; ++kk) {
+        const int d = lane + 32 * kk - am[kk];
+        const float tot = lvalid(kk) ? addH[kk] : 0.0f;
+        v4[1] += (static_cast<unsigned>(d + 1) > 2u) ? tot : 0.0f;
+        v4[2] += (d == -1) ? tot : 0.0f;
+        v4[3] += (d == 1) ? tot : 0.0f;
+      }
+      const float r = warp_reduce_scatter4(v4, lane);
+      const int q = (lane >> 3) & 3;
+      if ((lane & 7) == 0 && q >= 1) {
+        const int bb = (q == 1) ? 1 : (q == 2 ? 2 : 4);
+        ge = tile[bb * 33 + j] * r;
+        if (r != 0.0f) atomicAdd(gjump_fd + static_cast<int64_t>(bb) * HW + p, w * r);
+      }
+      if (lane == 0) rowH[gd] += r;  // no other lane touches label gd
+      ge = warp_sum(ge);
+      if (lane == 0 && ge != 0.0f) atomicAdd(gedge_fd + p, ge);
+    } else if (stereo) {
       constexpr int NB = (LV > 0) ? LV : 16;
       const int lv = (LV == 6 || LV == 8) ? LV : a.Lv;
       float bins[NB];
@@ -552,6 +585,10 @@ int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
   for (int phase = 0; phase < 2; ++phase) {
     BPL_TRACE(phase == 0 ? "lbp_backward: horizontal sweeps" : "lbp_backward: vertical sweeps");
     auto kern = (phase == 0) ? lbp_backward_kernel<K, V, LV, false, T> : lbp_backward_kernel<K, V, LV, true, T>;
+    if constexpr (V == BPL_LBP_STEREO && LV == 6 && K <= 8) {
+      if (a.layer_taps)
+        kern = (phase == 0) ? lbp_backward_kernel<K, V, LV, false, T, true> : lbp_backward_kernel<K, V, LV, true, T, true>;
+    }
     const int wmax = (phase == 0) ? bwd_warps_per_block<false, K>() : bwd_warps_per_block<true, K>();
     const int wpb = std::max(1, std::min(wmax, (200 * 1024) / per_warp));
     const size_t smem = static_cast<size_t>(per_warp) * wpb;

@@ -206,15 +206,20 @@ int bpl_lbp_backward_passes_f16(int variant, const float* jump, const float* edg
  * in_grad.  The layer's fused backward passes the buffer holding the
  * gradient of the probability volume (cost = -prob) from the belief
  * epilogue, with cost_sign -1, so the sum and the negation of the two cost
- * gradients cost no extra pass.  No counterpart in the reference (autograd
- * adds the cost's gradients there).
+ * gradients cost no extra pass.  layer_taps = 1 (stereo, Lv = 6): jump is
+ * the layer's packed taps [offset, L2, L1-, 0, L1+, L2] (taps 1 and 5 equal,
+ * tap 3 zero), and grad_jump receives what the layer's fold needs: the two
+ * L2 taps' gradient summed in tap 1, none in taps 3 and 5
+ * (message_passing_op_cuda.py:75-93 adds taps 1 and 5 and drops tap 3).
+ * No counterpart in the reference (autograd adds the cost's gradients
+ * there).
  */
 int bpl_lbp_backward_passes_into(int storage, int variant, const float* jump, const float* edge, const void* in_grad,
                                  int64_t in_grad_batch_stride, int64_t in_grad_slot_stride, const void* messages,
                                  const void* argmin, int argmin_kind, const float* scale, float* grad_cost,
                                  int grad_cost_ls, float cost_sign, float* grad_jump, float* grad_edge,
                                  void* workspace, size_t workspace_bytes, int B, int H, int W, int L, int Lv,
-                                 int jump_batch, int edge_batch, int passes, void* stream);
+                                 int jump_batch, int edge_batch, int passes, int layer_taps, void* stream);
 
 /*
  * Exact adjoint of one LBP pass (FP32 storage).  No counterpart in the

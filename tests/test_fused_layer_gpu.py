@@ -81,3 +81,52 @@ def test_half_padded_matches_torch():
         got = ops.half_padded(x, -1.0)
         want = ops.to_half_padded(-x, L)
         assert got.shape == want.shape and torch.equal(got, want)
+
+
+@pytest.mark.parametrize("half", [False, True])
+def test_layer_taps_adjoint_matches_the_plain_taps(half):
+    """bpl_lbp_backward_passes_into with layer_taps: the layer's packed taps
+    [offset, L2, L1, 0, L1, L2] binned three ways.  Against the plain
+    adjoint: tap 1 = taps 1 + 5, taps 2 and 4 and the edge and cost
+    gradients equal up to float order, taps 3 and 5 none."""
+    from bpl_gb300 import ops
+    from bpl_gb300.layers.stereo import pack_affinities
+    prob, edge, up, _ = _inputs(5, 2, 20, 44, 70)
+    dev = prob.device
+    B, H, W, L = prob.shape
+    aff = 0.05 + 0.5 * torch.rand((B, 4, 3, H, W), device=dev, generator=torch.Generator(device=dev).manual_seed(3))
+    taps = pack_affinities(aff, torch.zeros((B, 4, H, W), device=dev))
+    Ls = ops.padded_labels(L) if half else L
+    P = 2
+    am = torch.empty((P, B, 4, H, W, Ls), dtype=torch.uint8, device=dev)
+    if half:
+        cost = ops.half_padded(prob, -1.0)
+        m = torch.zeros((B, 4, H, W, Ls), dtype=torch.float16, device=dev)
+        for k in range(P):
+            ops.lbp_forward_f16(ops.LBP_STEREO, cost, taps, edge, m, 3, L, argmin_dtype=torch.uint8, argmin=am[k])
+        sc = None
+        gin = ops.half_padded(up).unsqueeze(1).expand(B, 4, H, W, Ls)
+    else:
+        cost = (-prob).contiguous()
+        m = torch.zeros((B, 4, H, W, L), device=dev)
+        sc = torch.empty((P, B, 4, H, W), device=dev)
+        for k in range(P):
+            ops.lbp_forward(ops.LBP_STEREO, cost, taps, edge, m, 3, argmin_dtype=torch.uint8, argmin=am[k],
+                            scale=sc[k])
+        gin = up.unsqueeze(1).expand(B, 4, H, W, L)
+    g0 = torch.zeros((B, H, W, L), device=dev)
+    g1 = torch.zeros((B, H, W, L), device=dev)
+    c0, j0, e0 = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, gin, m, am, sc, L=L, grad_cost_into=g0)
+    c1, j1, e1 = ops.lbp_backward_passes(ops.LBP_STEREO, taps, edge, gin, m, am, sc, L=L, grad_cost_into=g1,
+                                         layer_taps=True)
+
+    def close(a, b, name):
+        scale = b.abs().max().item()
+        err = (a - b).abs().max().item()
+        assert err <= 1e-5 * max(scale, 1e-30) + 1e-7, f"{name}: {err:.3e} of {scale:.3e}"
+    close(c1, c0, "grad_cost")
+    close(e1, e0, "grad_edge")
+    close(j1[:, :, 1], j0[:, :, 1] + j0[:, :, 5], "tap 1 + 5")
+    close(j1[:, :, 2], j0[:, :, 2], "tap 2")
+    close(j1[:, :, 4], j0[:, :, 4], "tap 4")
+    assert bool((j1[:, :, 3] == 0).all()) and bool((j1[:, :, 5] == 0).all())
