@@ -60,51 +60,90 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region.
+
+    Samples every 20 ms, each with nvidia-smi's own timestamp; sampling is
+    running before the region starts (the first sample has arrived), and the
+    summary keeps the samples taken between start() and stop().  A region
+    shorter than the sampling interval keeps the first sample after start()."""
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    INTERVAL_MS = 20
 
     def __init__(self, index):
         self.index = index
         self.proc = None
+        self.lines = []
+        self.t_start = self.t_stop = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.time(), line))
 
     def __enter__(self):
+        import threading
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
+            return self
+        self.reader = threading.Thread(target=self._read, daemon=True)
+        self.reader.start()
+        deadline = time.time() + 15.0
+        while not self.lines and time.time() < deadline and self.proc.poll() is None:
+            time.sleep(0.01)
         return self
 
+    def start(self):
+        self.t_start = time.time()
+
+    def stop(self):
+        self.t_stop = time.time()
+
     def __exit__(self, *exc):
-        self.out = ""
         if self.proc is not None:
             self.proc.terminate()
             try:
-                self.out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+            self.reader.join(timeout=5)
         return False
 
+    @staticmethod
+    def _stamp(text, arrival):
+        import datetime
+        try:
+            return datetime.datetime.strptime(text, "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return arrival
+
     def summary(self):
-        sms, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in (self.out or "").strip().splitlines():
+        rows = []
+        for arrival, line in self.lines:
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 8:
+            if len(f) < 9:
                 continue
             try:
-                sms.append(float(f[0]))
-                mx = float(f[1])
+                rows.append((self._stamp(f[0], arrival), float(f[1]), float(f[2]), f[5:9]))
             except ValueError:
                 continue
-            for n, v in zip(names, f[4:8]):
-                if v.lower().startswith("active"):
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
-                "samples": len(sms), "reasons": sorted(reasons)}
+        t0 = self.t_start if self.t_start is not None else float("-inf")
+        t1 = self.t_stop if self.t_stop is not None else float("inf")
+        inside = [r for r in rows if t0 <= r[0] <= t1]
+        if not inside:
+            inside = [r for r in rows if r[0] >= t0][:1]
+        sms = [r[1] for r in inside]
+        reasons = {n for r in inside for n, v in zip(names, r[3]) if v.lower().startswith("active")}
+        return {"sm_mhz": statistics.median(sms) if sms else None,
+                "sm_max_mhz": inside[-1][2] if inside else None,
+                "samples": len(sms), "interval_ms": self.INTERVAL_MS,
+                "region_s": (t1 - t0) if self.t_start is not None and self.t_stop is not None else None,
+                "reasons": sorted(reasons)}
 
 
 def synth_inputs(torch, dev, seed, H=H, W=W):
@@ -173,12 +212,14 @@ def run_ours(args):
     with ClockSampler(local) as clk, ops.timing() as tm:
         barrier()
         torch.cuda.profiler.start()  # profiler range = the timed region (ncu --profile-from-start off)
+        clk.start()
         t0.record(stream)
         for _ in range(args.steps):
             prob.grad = None
             step(prob, edge, upstream)
         t1.record(stream)
         barrier()
+        clk.stop()
         torch.cuda.profiler.stop()
     ms = t0.elapsed_time(t1)
     per_op = tm.report()
@@ -859,7 +900,8 @@ def run_reference(args):
 
 def run_ncu_case(args):
     """Small cases for detailed ncu captures, inside a profiler range (the
-    second run of each): LBP forward and reference adjoint at 256x512x192
+    second run of each): the layer's batched adjoint of ITERS passes (packed
+    taps) at 256x512x192, LBP forward and reference adjoint at 256x512x192
     (cost 100 MB, messages 400 MB: larger than L2, well under the capture
     size limit), the exact adjoint's message-gradient assembly, the belief
     epilogue, SAD at 384x512 C=64 D=192, the flow SAD at 384x512 C=32,
@@ -896,10 +938,26 @@ def run_ncu_case(args):
     gP = torch.rand((1, 4, 19, 19), device=dev)
     gm = torch.zeros((1, 4, 2 * h, 2 * w, 19), device=dev)
     gh = ops.to_half_padded(gin, L)
+    # the adjoint as the layer's step runs it: the layer's packed taps
+    # ([offset, L2, L1, 0, L1, L2] from the L1/L2 affinities) and the ITERS
+    # passes' indices in one launch, the cost gradient added into a buffer
+    aff = torch.zeros((1, 4, 3, h, w), device=dev)
+    aff[:, :, :2] = 0.1
+    aff[:, :, 2] = 0.5
+    lt = ops.pack_taps(aff, torch.zeros((1, 4, h, w), device=dev))
+    m3 = torch.zeros((1, 4, h, w, L), device=dev)
+    am3 = torch.empty((ITERS, 1, 4, h, w, L), dtype=torch.uint8, device=dev)
+    sc3 = torch.empty((ITERS, 1, 4, h, w), device=dev)
+    for k in range(ITERS):
+        ops.lbp_forward(ops.LBP_STEREO, cost, lt, edge, m3, DELTA, argmin_dtype=torch.uint8, argmin=am3[k],
+                        scale=sc3[k])
+    gc3 = torch.zeros((1, h, w, L), device=dev)
     for it in range(2):
         if it == 1:
             torch.cuda.synchronize()
             torch.cuda.profiler.start()
+        ops.lbp_backward_passes(ops.LBP_STEREO, lt, edge, gin, m3, am3, sc3, L=L, grad_cost_into=gc3,
+                                cost_sign=-1.0, layer_taps=True)
         m, am, sc = ops.lbp_forward(ops.LBP_STEREO, cost, jump, edge, m, DELTA, argmin_dtype=torch.uint8)
         ops.lbp_backward(ops.LBP_STEREO, jump, edge, gin, m, am, sc, copy_grad_messages=False)
         ops.lbp_backward(ops.LBP_STEREO, jump, edge, gin, m, am, sc, mode="exact")

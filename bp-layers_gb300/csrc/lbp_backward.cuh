@@ -583,7 +583,7 @@ int launch_bwd_k(const BwdArgs& a0, cudaStream_t stream) {
   BwdArgs a = a0;
   const int per_warp = bwd::warp_smem_floats(K, a.ns, a.lrow, a.Lv, a.L, V, sizeof(T)) * 4;
   for (int phase = 0; phase < 2; ++phase) {
-    BPL_TRACE(phase == 0 ? "lbp_backward: horizontal sweeps" : "lbp_backward: vertical sweeps");
+    BPL_TRACE(phase == 0 ? "lbp_backward: vertical sweeps" : "lbp_backward: horizontal sweeps");
     auto kern = (phase == 0) ? lbp_backward_kernel<K, V, LV, false, T> : lbp_backward_kernel<K, V, LV, true, T>;
     if constexpr (V == BPL_LBP_STEREO && LV == 6 && K <= 8) {
       if (a.layer_taps)

@@ -647,15 +647,22 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
 
     if (kPcolRegs && delta >= L) {
       // full minimisation with the register column (see kPcolRegs); same
-      // order and tie rule as below
+      // order and tie rule as below.  Senders go in groups of four, one
+      // label-count test per group: a sender s >= L in the last group has
+      // h = +inf and a zero column entry, so its term is +inf (or NaN when
+      // w is infinite) and neither lowers the minimum nor equals it.
       float m = 1e15f;
       int arg = 0;
 #pragma unroll
-      for (int s = 0; s < 32; ++s) {
-        if (s < L) {
-          const float nm = __fmaf_rn(pcol[s], w, cs.hs[s]);
-          m = fminf(m, nm);
-          if (m == nm) arg = s;
+      for (int g = 0; g < 8; ++g) {
+        if (4 * g < L) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int s = 4 * g + q;
+            const float nm = __fmaf_rn(pcol[s], w, cs.hs[s]);
+            m = fminf(m, nm);
+            if (m == nm) arg = s;
+          }
         }
       }
       msg[0] = (lane < L) ? m : 1e15f;
