@@ -647,23 +647,34 @@ __global__ void __launch_bounds__(32 * fwd_block_warps<OCC>(), OCC) lbp_forward_
 
     if (kPcolRegs && delta >= L) {
       // full minimisation with the register column (see kPcolRegs); same
-      // order and tie rule as below.  Senders go in groups of four, one
-      // label-count test per group: a sender s >= L in the last group has
-      // h = +inf and a zero column entry, so its term is +inf (or NaN when
-      // w is infinite) and neither lowers the minimum nor equals it.
-      float m = 1e15f;
-      int arg = 0;
+      // order and tie rule as below.  The 32 senders run as four
+      // independent chains over the contiguous ranges [8c, 8c+8), combined
+      // in sender order: the minimum's value (a left fold of fminf over the
+      // senders in order, whatever fminf returns for equal operands) and
+      // the last sender that attains it are those of the single chain.
+      // Senders s >= L have h = +inf and a zero column entry: their terms
+      // are +inf (NaN for an infinite w) and neither lower a minimum nor
+      // equal it, so they need no test.
+      float mc[4] = {1e15f, kInf, kInf, kInf};
+      int ac[4] = {0, 0, 0, 0};
 #pragma unroll
-      for (int g = 0; g < 8; ++g) {
-        if (4 * g < L) {
+      for (int q = 0; q < 8; ++q) {
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int s = 4 * g + q;
-            const float nm = __fmaf_rn(pcol[s], w, cs.hs[s]);
-            m = fminf(m, nm);
-            if (m == nm) arg = s;
-          }
+        for (int ch = 0; ch < 4; ++ch) {
+          const int s = 8 * ch + q;
+          const float nm = __fmaf_rn(pcol[s], w, cs.hs[s]);
+          mc[ch] = fminf(mc[ch], nm);
+          if (mc[ch] == nm) ac[ch] = s;
         }
+      }
+      float m = mc[0];
+      int arg = ac[0];
+#pragma unroll
+      for (int ch = 1; ch < 4; ++ch) {
+        m = fminf(m, mc[ch]);
+        // chain ch holds a sender at the minimum (it started at +inf, the
+        // minimum is at most 1e15): its last such sender is the latest
+        arg = (mc[ch] == m) ? ac[ch] : arg;
       }
       msg[0] = (lane < L) ? m : 1e15f;
       am[0] = (lane < L) ? arg : 0;
