@@ -139,6 +139,26 @@ def test_semantic_forward_matches_oracle(case):
     assert_parity(gpu, ref, name)
 
 
+# The global variant with one label per lane (L <= 32) minimises over the
+# senders as four chains over [8c, 8c+8), combined in sender order;
+# quantised costs, messages, matrix and weights put exact ties (and negative
+# zeros) on both sides of the chain boundaries.
+GLOBAL_TIE_LS = [1, 7, 8, 9, 15, 16, 17, 24, 25, 31, 32]
+
+
+@pytest.mark.parametrize("L", GLOBAL_TIE_LS)
+def test_semantic_global_register_column_ties(L):
+    g = cases.rng(500 + L)
+    B, H, W = 2, 9, 40
+    cost = cases.random_cost(g, B, H, W, L, quantise=4)
+    jump, _ = cases.semantic_global_jump(g, L, quantise=2)
+    edge = cases.edge_weights(g, B, H, W, quantise=2)
+    msgs = cases.random_messages(g, B, H, W, L, quantise=4)
+    gpu = _run_gpu(1, cost, jump, edge, msgs, L, 2)
+    ref = oracle.lbp_forward(1, cost, jump, edge, msgs, L, iters=2)
+    assert_parity(gpu, ref, f"global_ties_l{L}")
+
+
 def test_small_config_forward():
     """96x128, 32 labels, one pass, as the small stereo workload."""
     g = cases.rng(0)
