@@ -285,17 +285,6 @@ def run_ours(args):
 
     e2e_run(max(2, args.warmup // 2))
     barrier()
-    # Warm the input copy stream right before the region: started straight
-    # after the barrier (device idle), 10-step runs took 3-4 ms per step
-    # longer in 2 of 3 trials; after one 64 MB host-to-device copy on the
-    # same stream, synchronised, 3 of 3 trials ran at the steady rate.  The
-    # copy lands in a scratch buffer outside the timed region; every timed
-    # step still copies all of its own inputs.
-    warm = torch.empty(16 * 1024 * 1024, device=dev)
-    with torch.cuda.stream(cin):
-        warm.copy_(prob_h.view(-1)[:warm.numel()], non_blocking=True)
-    cin.synchronize()
-    del warm
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
